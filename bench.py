@@ -1,0 +1,306 @@
+#!/usr/bin/env python3
+"""Benchmark of the entropical GB300 density hot path.
+
+Workload (one step): all-pairs mutual information over 64 coordinates x
+100,000 frames -- 64 1-D marginal densities and 2,016 2-D joint densities,
+Scott-rule bandwidths, resubstitution MI -- computed as ONE batch through the
+library (one persistent pair-kernel launch per dimension). Synthetic, seeded
+data: x_t = tanh(A z_t), z a 16-dim AR(1) (phi 0.95), columns standardised.
+
+value      in-support pair-kernel evaluations per second, inputs resident in
+           HBM (ent_mi_all_pairs_device), device time on the library stream
+e2e        same metric through the host-buffer C-ABI call ent_mi_all_pairs,
+           host->device copy of the coordinates and device->host copy of the
+           MI matrix inside the timed region
+roofline   the dominant kernel (2-D pair kernel) against the FP32 CUDA-core
+           peak: 10 flops per evaluated (target, candidate) pair
+cpu_baseline  the reference's OpenMP density algorithm (restated in C with
+           its own linear window scans, all host cores) on a bounded sample
+
+--impl reference times that CPU implementation alone (the reference arm).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "pair-kernel evals/s; MI/TE estimates/s batched+learned vs plain at |ΔH|≤1e-4 nats"
+UNIT = "pair-kernel evals/s"
+N_FRAMES, N_COORDS = 100_000, 64
+WORKLOAD = "all-pairs MI, 64 coords x 100k frames, tanh(A z) AR(1) latent, Scott h"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except Exception:
+                self.p.kill()
+
+    def summary(self):
+        self.f.flush()
+        rows = []
+        for ln in Path(self.f.name).read_text().splitlines():
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows),
+                "sm_max_mhz": max(r[1] for r in rows), "reasons": reasons, "samples": len(rows)}
+
+
+def fp32_peak_tflops(n_sms: int) -> tuple[float, str]:
+    mhz = 2070.0
+    try:
+        mp = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+        mhz = float(mp.get("sm_max_mhz", mhz))
+    except Exception:
+        pass
+    peak = n_sms * 128 * 2 * mhz * 1e6 / 1e12
+    return peak, (f"nominal FP32 CUDA-core peak {n_sms} SMs x 128 FMA/clk x 2 x {mhz:.0f} MHz "
+                  "(no measured FP32 figure in MEASURED_PEAKS.json)")
+
+
+def ncu_traffic() -> float | None:
+    """DRAM bytes per launch of the 2-D pair kernel from the committed ncu
+    summary (profiles/), if one has been captured."""
+    p = ROOT / "profiles" / "density2d_mi64x100k_ncu.txt"
+    if not p.exists():
+        return None
+    for ln in p.read_text().splitlines():
+        if ln.startswith("dram_bytes_per_launch"):
+            try:
+                return float(ln.split("=", 1)[1].split()[0])
+            except Exception:
+                return None
+    return None
+
+
+def cpu_port_sample(x: np.ndarray, h: np.ndarray, pairs, support):
+    """Time the reference OpenMP density algorithm (restated, with its linear
+    window scans) on the given instances; returns (pairs/s, seconds, n)."""
+    from oracle import oracle as O
+    t0 = time.perf_counter()
+    for inst in pairs:
+        O.density_ref_f32(O.repack(x, list(inst)), [h[c] for c in inst], linear_scan=True)
+    dt = time.perf_counter() - t0
+    return support / dt, dt
+
+
+def reference_arm(args, x, h):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    pairs = [(0, 1), (2, 3), (4, 5), (6, 7), (8, 9), (10, 11)]
+    rates, times = [], []
+    for s in range(args.warmup + args.steps):
+        i, j = pairs[s % len(pairs)]
+        sel = O.repack(x, [i, j])
+        support = O.support_count_fp64(sel, [h[i], h[j]])
+        rate, dt = cpu_port_sample(x, h, [(i, j)], support)
+        if s >= args.warmup:
+            rates.append(rate)
+            times.append(dt)
+    v = statistics.mean(rates)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "step": "one 2-D joint density of one column pair, N=100k",
+                   "parallelism": f"OpenMP {cores} host threads"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "one 2-D pair density per step at N=100k, reference OpenMP "
+                                   "algorithm restated in C (linear window scans kept)"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_env()
+    from entropical_gb300 import workloads
+    x = workloads.mi_coords(N_FRAMES, N_COORDS, seed=2024)
+    h = workloads.scott_bandwidth(x, 2)
+    if args.impl == "reference":
+        return reference_arm(args, x, h)
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist_mod
+        dist_mod.init_process_group("nccl")
+        dist = dist_mod
+    from entropical_gb300 import Context
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    ctx = Context(local)
+    n_sms = torch.cuda.get_device_properties(local).multi_processor_count
+    dx = torch.from_numpy(x).cuda(local)
+    ptr = dx.data_ptr()
+    iu = np.triu_indices(N_COORDS, 1)
+
+    # work units of the step: in-support (target, source) pairs (untimed)
+    cnt, c1 = ctx.mi_all_pairs_device(ptr, N_FRAMES, N_COORDS, h, counts=True)
+    support_2d = float(cnt[iu].sum())
+    support_1d = float(c1.sum())
+    support = support_2d + support_1d
+
+    for _ in range(args.warmup):
+        mi, hx = ctx.mi_all_pairs_device(ptr, N_FRAMES, N_COORDS, h)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+
+    step_ms, k2_ms, k2_pairs, k1_ms, launches = [], [], [], [], 0
+    barrier()
+    wall0 = time.perf_counter()
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()  # L2 flush between steps (256 MB > 129 MB L2)
+            torch.cuda.synchronize()
+            mi, hx = ctx.mi_all_pairs_device(ptr, N_FRAMES, N_COORDS, h)
+            st = ctx.last_stats()
+            step_ms.append(st.total_ms)
+            k2_ms.append(st.pair_kernel_ms_by_dim[1])
+            k1_ms.append(st.pair_kernel_ms_by_dim[0])
+            k2_pairs.append(st.candidate_pairs_by_dim[1])
+            launches += st.kernel_launches
+    barrier()
+    wall = time.perf_counter() - wall0
+    ms = statistics.mean(step_ms)
+    if dist is not None:
+        t = torch.tensor([ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = support * ws / (ms / 1e3)
+
+    # end to end through the host-buffer call (pinned host input)
+    xp = torch.from_numpy(x).pin_memory()
+    xnp = xp.numpy()
+    e2e_ms = []
+    for s in range(args.warmup + args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        mi_e, hx_e = ctx.mi_all_pairs(xnp, h)
+        w = (time.perf_counter() - t0) * 1e3
+        if s >= args.warmup:
+            e2e_ms.append(max(w, ctx.last_stats().total_ms))
+    e2e = statistics.mean(e2e_ms)
+    assert np.allclose(mi_e, mi, rtol=0, atol=1e-9)
+
+    if rank != 0:
+        return
+    peak, peak_note = fp32_peak_tflops(n_sms)
+    t2 = statistics.mean(k2_ms) / 1e3
+    achieved = 10.0 * statistics.mean(k2_pairs) / t2 / 1e12
+    traffic = ncu_traffic()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n_frames": N_FRAMES, "n_coords": N_COORDS,
+                   "densities_per_step": N_COORDS + len(iu[0]), "l2": "flushed (256 MB write) "
+                   "between steps", "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "mi_estimates_per_s": len(iu[0]) * ws / (ms / 1e3),
+        "support_pairs_per_step": support,
+        "candidate_pairs_2d_per_step": statistics.mean(k2_pairs),
+        "pair_kernel_ms": {"d1": statistics.mean(k1_ms), "d2": statistics.mean(k2_ms)},
+        "wall_s_timed": wall,
+        "clocks": clk.summary(),
+        "e2e": {"value": support / (e2e / 1e3), "unit": UNIT,
+                "h2d_bytes_per_step": int(x.nbytes), "d2h_bytes_per_step": int(mi.nbytes + hx.nbytes),
+                "ms_per_step": e2e},
+        "gpu_launches": launches,
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": "k_density<2,16> (2-D pair kernel)",
+                     "flops_per_pair": 10, "peak_kind": peak_note},
+    }
+    if not args.no_cpu_baseline and ws == 1:
+        try:
+            from oracle import oracle as O
+            O.build_oracle() if not O.ORACLE_SO.exists() else None
+            cores = os.cpu_count() or 1
+            sample = [(0,), (0, 1)]
+            sup = float(c1[0] + cnt[0, 1])
+            rate, dt = cpu_port_sample(x, h, sample, sup)
+            line["cpu_baseline"] = {
+                "value": rate, "unit": UNIT, "cores": cores, "kind": "port", "seconds": dt,
+                "sample": "1-D marginal of column 0 + 2-D joint of columns (0,1), N=100k; "
+                          "reference OpenMP algorithm restated in C, its linear window scans kept",
+                "extrapolated_job_s": support / rate}
+        except Exception as exc:  # the baseline is reported, never required
+            line["cpu_baseline"] = {"value": None, "error": str(exc)[:200]}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

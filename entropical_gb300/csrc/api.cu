@@ -1,0 +1,638 @@
+// C ABI and host orchestration of the entropical GB300 density path.
+//
+// A context (ent_ctx) owns one stream, a grow-only device workspace and the
+// statistics of the last call. Every density request is expressed as a batch
+// of instances over column views and run by Engine::run:
+//
+//   views  --colstats-->  min/max/moments (one host sync)
+//          --radix sort--> dimension-0 order per view
+//   insts  --strip keys + stable radix--> strip-major order, strip starts
+//          --tile offsets, gather, plan--> tile descriptors
+//          --persistent pair kernel (per d)--> densities / log-sums
+//
+// The plain combined_densities() replacement is a batch of one instance;
+// the batched estimators (mi, transs, uneven entropy batches) submit all of
+// their instances at once so that one persistent launch per dimension covers
+// every (instance, tile) work item.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/entropical_gb300.h"
+#include "api_internal.h"
+#include "engine.h"
+
+using namespace ent;
+
+// ------------------------------------------------------------------ arena
+void* Arena::alloc(size_t bytes) {
+  bytes = (bytes + 255) & ~(size_t)255;
+  if (bytes == 0) bytes = 256;
+  if (!blocks.empty() && used_in_last + bytes <= blocks.back().size) {
+    void* p = static_cast<char*>(blocks.back().ptr) + used_in_last;
+    used_in_last += bytes;
+    total_used += bytes;
+    return p;
+  }
+  size_t sz = std::max(bytes, blocks.empty() ? (size_t)64 << 20
+                                             : blocks.back().size * 2);
+  void* p = nullptr;
+  if (cudaMalloc(&p, sz) != cudaSuccess) {
+    cudaGetLastError();
+    sz = bytes;
+    if (cudaMalloc(&p, sz) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+  }
+  blocks.push_back({p, sz});
+  used_in_last = bytes;
+  total_used += bytes;
+  return p;
+}
+
+void Arena::reset() {
+  if (blocks.size() > 1) {
+    size_t want = std::max(total_used, (size_t)64 << 20);
+    for (auto& b : blocks) cudaFree(b.ptr);
+    blocks.clear();
+    void* p = nullptr;
+    if (cudaMalloc(&p, want) == cudaSuccess) blocks.push_back({p, want});
+    else cudaGetLastError();
+  }
+  used_in_last = 0;
+  total_used = 0;
+}
+
+void Arena::release() {
+  for (auto& b : blocks) cudaFree(b.ptr);
+  blocks.clear();
+  used_in_last = total_used = 0;
+}
+
+// ---------------------------------------------------------------- context
+int Ctx::fail(int status, const std::string& msg) {
+  last_error = msg;
+  return status;
+}
+
+int Ctx::cuda_fail(cudaError_t e, const char* where) {
+  last_error = std::string("CUDA error: ") + where + "\n" + cudaGetErrorString(e);
+  return ENT_ERR_CUDA;
+}
+
+int Ctx::begin_call() {
+  last_error.clear();
+  stats = ent_call_stats{};
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  e = cudaStreamSynchronize(stream);
+  if (e != cudaSuccess) return cuda_fail(e, "stream sync");
+  arena.reset();
+  e = cudaMemsetAsync(d_err, 0, sizeof(uint32_t), stream);
+  if (e != cudaSuccess) return cuda_fail(e, "memset err");
+  cudaEventRecord(ev_call0, stream);
+  return ENT_OK;
+}
+
+int Ctx::end_call() {
+  cudaEventRecord(ev_call1, stream);
+  cudaError_t e = cudaStreamSynchronize(stream);
+  if (e != cudaSuccess) return cuda_fail(e, "kernel execution");
+  uint32_t err = 0;
+  e = cudaMemcpy(&err, d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "read error word");
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, ev_call0, ev_call1) == cudaSuccess)
+    stats.total_ms = ms;
+  cudaGetLastError();
+  if (err & EF_TIMEOUT)
+    return fail(ENT_ERR_TIMEOUT, "a bounded device-side wait expired");
+  if (err & EF_NONFINITE)
+    return fail(ENT_ERR_NONFINITE, "non-finite coordinate in the selection");
+  return ENT_OK;
+}
+
+// ----------------------------------------------------------------- engine
+namespace {
+
+template <class T>
+T* arena_upload(Ctx& c, const std::vector<T>& v, cudaError_t* e) {
+  T* p = static_cast<T*>(c.arena.alloc(sizeof(T) * std::max<size_t>(v.size(), 1)));
+  if (!p) {
+    *e = cudaErrorMemoryAllocation;
+    return nullptr;
+  }
+  if (!v.empty())
+    *e = cudaMemcpyAsync(p, v.data(), sizeof(T) * v.size(),
+                         cudaMemcpyHostToDevice, c.stream);
+  else
+    *e = cudaSuccess;
+  return p;
+}
+
+// Segment table for the segmented radix sort over (offset, length) pairs.
+struct SegBuild {
+  std::vector<uint64_t> off;
+  std::vector<uint32_t> len, blk0, blk_seg;
+  uint32_t total_blocks = 0;
+  void add(uint64_t o, uint32_t n) {
+    off.push_back(o);
+    len.push_back(n);
+    blk0.push_back(total_blocks);
+    const uint32_t nb = radix_blocks_for(n);
+    for (uint32_t i = 0; i < nb; ++i) blk_seg.push_back((uint32_t)len.size() - 1);
+    total_blocks += nb;
+  }
+  int upload(Ctx& c, SegTableDev* t) {
+    cudaError_t e;
+    blk0.push_back(total_blocks);
+    t->seg_off = arena_upload(c, off, &e);
+    if (e != cudaSuccess) return c.cuda_fail(e, "upload seg_off");
+    t->seg_len = arena_upload(c, len, &e);
+    if (e != cudaSuccess) return c.cuda_fail(e, "upload seg_len");
+    t->seg_blk0 = arena_upload(c, blk0, &e);
+    if (e != cudaSuccess) return c.cuda_fail(e, "upload seg_blk0");
+    t->blk_seg = arena_upload(c, blk_seg, &e);
+    if (e != cudaSuccess) return c.cuda_fail(e, "upload blk_seg");
+    t->hist = static_cast<uint32_t*>(
+        c.arena.alloc(sizeof(uint32_t) * 256 * (size_t)std::max(total_blocks, 1u)));
+    if (!t->hist) return c.fail(ENT_ERR_CUDA, "out of device memory");
+    return ENT_OK;
+  }
+};
+
+int bits_for(uint32_t max_key) {
+  int b = 0;
+  while (b < 32 && (max_key >> b) != 0) ++b;
+  return ((b + 7) / 8) * 8;
+}
+
+}  // namespace
+
+int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
+                std::vector<InstSpec>& insts, uint32_t mode, EngineOut* out) {
+  cudaError_t e;
+  const cudaStream_t st = c.stream;
+  const uint32_t nv = (uint32_t)views.size();
+  const uint32_t ni = (uint32_t)insts.size();
+  if (nv == 0 || ni == 0) return ENT_OK;
+  if (nv > 65535 || ni > 65535)
+    return c.fail(ENT_ERR_TOO_LARGE, "more than 65535 views or instances in one batch");
+
+  // 1. column statistics (one host round trip)
+  std::vector<ViewDev> hv(nv);
+  uint32_t max_vn = 0;
+  std::vector<uint64_t> voff(nv);
+  uint64_t vtot = 0;
+  for (uint32_t v = 0; v < nv; ++v) {
+    hv[v].x = views[v].x;
+    hv[v].n = views[v].n;
+    hv[v].pad = 0;
+    voff[v] = vtot;
+    vtot += views[v].n;
+    max_vn = std::max(max_vn, views[v].n);
+  }
+  ViewDev* dv = arena_upload(c, hv, &e);
+  if (e != cudaSuccess) return c.cuda_fail(e, "upload views");
+  ViewStats* dstats = static_cast<ViewStats*>(c.arena.alloc(sizeof(ViewStats) * nv));
+  if (!dstats) return c.fail(ENT_ERR_CUDA, "out of device memory");
+  e = launch_colstats(st, dv, nv, dstats);
+  if (e != cudaSuccess) return c.cuda_fail(e, "colstats");
+  c.stats.kernel_launches += 1;
+  std::vector<ViewStats> vs(nv);
+  e = cudaMemcpyAsync(vs.data(), dstats, sizeof(ViewStats) * nv,
+                      cudaMemcpyDeviceToHost, st);
+  if (e != cudaSuccess) return c.cuda_fail(e, "read stats");
+
+  // 2. value sort of every view (overlaps the stats read-back)
+  uint64_t* dvoff = arena_upload(c, voff, &e);
+  if (e != cudaSuccess) return c.cuda_fail(e, "upload view offsets");
+  uint32_t* vk = static_cast<uint32_t*>(c.arena.alloc(4 * vtot));
+  uint32_t* vvals = static_cast<uint32_t*>(c.arena.alloc(4 * vtot));
+  uint32_t* vk2 = static_cast<uint32_t*>(c.arena.alloc(4 * vtot));
+  uint32_t* vv2 = static_cast<uint32_t*>(c.arena.alloc(4 * vtot));
+  if (!vk || !vvals || !vk2 || !vv2) return c.fail(ENT_ERR_CUDA, "out of device memory");
+  e = launch_view_keys(st, dv, dvoff, nv, max_vn, vk, vvals);
+  if (e != cudaSuccess) return c.cuda_fail(e, "view keys");
+  c.stats.kernel_launches += 1;
+  {
+    SegBuild sb;
+    for (uint32_t v = 0; v < nv; ++v) sb.add(voff[v], views[v].n);
+    SegTableDev t;
+    int s = sb.upload(c, &t);
+    if (s) return s;
+    e = seg_radix_sort(st, t, nv, sb.total_blocks, vk, vvals, vk2, vv2, 0, 32);
+    if (e != cudaSuccess) return c.cuda_fail(e, "view sort");
+    c.stats.kernel_launches += 12;
+  }
+  e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return c.cuda_fail(e, "colstats/sort");
+  for (uint32_t v = 0; v < nv; ++v)
+    if (vs[v].nonfinite)
+      return c.fail(ENT_ERR_NONFINITE, "non-finite coordinate in the selection");
+
+  // 3. host plan of every instance
+  std::vector<InstDev> hi(ni);
+  std::vector<uint32_t> order;  // instances grouped by dimension
+  for (int d = 1; d <= 3; ++d)
+    for (uint32_t i = 0; i < ni; ++i)
+      if ((int)insts[i].d == d) order.push_back(i);
+  uint32_t slot = 0;
+  uint32_t max_n = 0;
+  uint32_t max_strips = 1;
+  for (int d = 1; d <= 3; ++d) {
+    group_base[d] = slot;
+    for (uint32_t i : order) {
+      InstSpec& s = insts[i];
+      if ((int)s.d != d) continue;
+      InstDev& I = hi[i];
+      std::memset(&I, 0, sizeof(I));
+      I.n = s.n;
+      I.d = s.d;
+      max_n = std::max(max_n, s.n);
+      double prod_h = 1.0;
+      for (uint32_t j = 0; j < s.d; ++j) {
+        const ViewStats& st_j = vs[s.view[j]];
+        I.x[j] = views[s.view[j]].x;
+        I.center[j] = 0.5f * (st_j.mn + st_j.mx);
+        I.inv_h[j] = 1.0f / s.h[j];
+        prod_h *= (double)s.h[j];
+      }
+      I.perm0 = vvals + voff[s.view[0]];
+      I.S = s.d == 2 ? std::max(1u, std::min(4u, s.S)) : 1u;
+      I.ncell1 = I.ncell2 = 1;
+      if (s.d >= 2) {
+        const ViewStats& a = vs[s.view[1]];
+        const double w = (double)s.h[1] / I.S * (1.0 + 1e-4);
+        I.lo1 = a.mn;
+        I.inv_w1 = 1.0 / w;
+        // Capping the cell count only merges far cells (more candidates,
+        // never fewer in-support sources).
+        I.ncell1 = (uint32_t)std::min<double>(
+            std::floor(((double)a.mx - (double)a.mn) / w) + 1.0,
+            s.d == 2 ? (1u << 16) : (1u << 10));
+      }
+      if (s.d == 3) {
+        const ViewStats& b = vs[s.view[2]];
+        const double w = (double)s.h[2] * (1.0 + 1e-4);
+        I.lo2 = b.mn;
+        I.inv_w2 = 1.0 / w;
+        I.ncell2 = (uint32_t)std::min<double>(
+            std::floor(((double)b.mx - (double)b.mn) / w) + 1.0, 1u << 10);
+      }
+      I.n_strips = I.ncell1 * I.ncell2;
+      max_strips = std::max(max_strips, I.n_strips);
+      I.tt = (uint32_t)density_tile_targets((int)s.d);
+      I.tile_cap = (s.n + I.tt - 1) / I.tt + std::min(I.n_strips, s.n);
+      I.tile_base = slot;
+      slot += I.tile_cap;
+      I.scale = std::pow(0.75, (double)s.d) / (s.norm * prod_h);
+      I.out = s.out;
+    }
+    group_slots[d] = slot - group_base[d];
+  }
+  const uint32_t n_slots = slot;
+
+  // buffers per instance
+  std::vector<uint32_t> seg_inst;  // d >= 2 instances (strip sort segments)
+  std::vector<uint64_t> seg_off;
+  uint64_t seg_tot = 0;
+  for (uint32_t i = 0; i < ni; ++i) {
+    InstDev& I = hi[i];
+    const size_t esz = I.d == 1 ? 4 : (I.d == 2 ? 8 : 16);
+    I.pts = c.arena.alloc(esz * ((size_t)I.n + 8));
+    I.strip_start = static_cast<uint32_t*>(c.arena.alloc(4 * ((size_t)I.n_strips + 1)));
+    I.tile_off = static_cast<uint32_t*>(c.arena.alloc(4 * ((size_t)I.n_strips + 1)));
+    if (!I.pts || !I.strip_start || !I.tile_off)
+      return c.fail(ENT_ERR_CUDA, "out of device memory");
+    if (I.d == 1) {
+      I.perm = const_cast<uint32_t*>(I.perm0);
+    } else {
+      seg_inst.push_back(i);
+      seg_off.push_back(seg_tot);
+      seg_tot += I.n;
+    }
+  }
+  uint32_t *sk = nullptr, *svals = nullptr, *sk2 = nullptr, *sv2 = nullptr;
+  int strip_bits = bits_for(max_strips);
+  if (!seg_inst.empty()) {
+    sk = static_cast<uint32_t*>(c.arena.alloc(4 * seg_tot));
+    svals = static_cast<uint32_t*>(c.arena.alloc(4 * seg_tot));
+    sk2 = static_cast<uint32_t*>(c.arena.alloc(4 * seg_tot));
+    sv2 = static_cast<uint32_t*>(c.arena.alloc(4 * seg_tot));
+    if (!sk || !svals || !sk2 || !sv2) return c.fail(ENT_ERR_CUDA, "out of device memory");
+    const int passes = strip_bits / 8;
+    uint32_t* rk = (passes % 2) ? sk2 : sk;
+    uint32_t* rv = (passes % 2) ? sv2 : svals;
+    for (size_t q = 0; q < seg_inst.size(); ++q) {
+      hi[seg_inst[q]].perm = rv + seg_off[q];
+      hi[seg_inst[q]].skeys = rk + seg_off[q];
+    }
+  }
+  InstDev* di = arena_upload(c, hi, &e);
+  if (e != cudaSuccess) return c.cuda_fail(e, "upload instances");
+
+  // 4. strip partition (stable, keeps dimension-0 order inside strips)
+  if (!seg_inst.empty()) {
+    uint32_t* dseg_inst = arena_upload(c, seg_inst, &e);
+    if (e != cudaSuccess) return c.cuda_fail(e, "upload seg inst");
+    uint64_t* dseg_off = arena_upload(c, seg_off, &e);
+    if (e != cudaSuccess) return c.cuda_fail(e, "upload seg off");
+    e = launch_strip_keys(st, di, dseg_inst, dseg_off, (uint32_t)seg_inst.size(),
+                          max_n, sk, svals);
+    if (e != cudaSuccess) return c.cuda_fail(e, "strip keys");
+    c.stats.kernel_launches += 1;
+    SegBuild sb;
+    for (size_t q = 0; q < seg_inst.size(); ++q) sb.add(seg_off[q], hi[seg_inst[q]].n);
+    SegTableDev t;
+    int s = sb.upload(c, &t);
+    if (s) return s;
+    uint32_t *k0 = sk, *v0 = svals, *k1 = sk2, *v1 = sv2;
+    e = seg_radix_sort(st, t, (uint32_t)seg_inst.size(), sb.total_blocks, k0, v0,
+                       k1, v1, 0, strip_bits);
+    if (e != cudaSuccess) return c.cuda_fail(e, "strip sort");
+    c.stats.kernel_launches += 3 * (strip_bits / 8);
+  }
+
+  // 5. strips, tiles, points, plan
+  e = launch_strip_bounds(st, di, ni, max_n);
+  if (e != cudaSuccess) return c.cuda_fail(e, "strip bounds");
+  e = launch_tile_offsets(st, di, ni);
+  if (e != cudaSuccess) return c.cuda_fail(e, "tile offsets");
+  e = launch_gather_pts(st, di, ni, max_n);
+  if (e != cudaSuccess) return c.cuda_fail(e, "gather points");
+  c.stats.kernel_launches += 3;
+  // instance index for every slot: inst_tile_base must be ascending, so the
+  // plan kernel searches the instances in slot order.
+  std::vector<uint32_t> slot_order(ni);
+  for (uint32_t i = 0; i < ni; ++i) slot_order[i] = i;
+  std::sort(slot_order.begin(), slot_order.end(),
+            [&](uint32_t a, uint32_t b) { return hi[a].tile_base < hi[b].tile_base; });
+  std::vector<InstDev> hi_sorted(ni);
+  std::vector<uint32_t> inst_base(ni);
+  for (uint32_t r = 0; r < ni; ++r) {
+    hi_sorted[r] = hi[slot_order[r]];
+    inst_base[r] = hi[slot_order[r]].tile_base;
+  }
+  InstDev* di_sorted = arena_upload(c, hi_sorted, &e);
+  if (e != cudaSuccess) return c.cuda_fail(e, "upload sorted instances");
+  uint32_t* dbase = arena_upload(c, inst_base, &e);
+  if (e != cudaSuccess) return c.cuda_fail(e, "upload tile bases");
+  TileDesc* tiles = static_cast<TileDesc*>(c.arena.alloc(sizeof(TileDesc) * (size_t)n_slots));
+  uint64_t* dnsrc = static_cast<uint64_t*>(c.arena.alloc(sizeof(uint64_t) * 3));
+  double* tile_ls = static_cast<double*>(c.arena.alloc(sizeof(double) * (size_t)n_slots));
+  uint32_t* wc = static_cast<uint32_t*>(c.arena.alloc(sizeof(uint32_t) * 4));
+  if (!tiles || !dnsrc || !tile_ls || !wc) return c.fail(ENT_ERR_CUDA, "out of device memory");
+  cudaMemsetAsync(dnsrc, 0, sizeof(uint64_t) * 3, st);
+  e = launch_plan(st, di_sorted, ni, dbase, tiles, n_slots, dnsrc);
+  if (e != cudaSuccess) return c.cuda_fail(e, "plan");
+  c.stats.kernel_launches += 1;
+
+  // 6. pair kernel, one persistent launch per dimension present.
+  // The tile descriptors carry indices into the slot-sorted instance array.
+  cudaEventRecord(c.ev_k0, st);
+  for (int d = 1; d <= 3; ++d) {
+    if (group_slots[d] == 0) continue;
+    int launched = 0;
+    cudaEventRecord(c.ev_d[d - 1][0], st);
+    e = launch_density(st, d, tiles + group_base[d], group_slots[d], di_sorted,
+                       wc + d, c.d_err, tile_ls + group_base[d], mode, c.n_sms,
+                       &launched);
+    if (e != cudaSuccess) return c.cuda_fail(e, "density kernel");
+    cudaEventRecord(c.ev_d[d - 1][1], st);
+    c.ran_d[d - 1] = true;
+    c.stats.kernel_launches += 1;
+  }
+  cudaEventRecord(c.ev_k1, st);
+  if (mode & (DM_LOGSUM | DM_SUMV)) {
+    double* dls = static_cast<double*>(c.arena.alloc(sizeof(double) * ni));
+    if (!dls) return c.fail(ENT_ERR_CUDA, "out of device memory");
+    e = launch_inst_logsum(st, di_sorted, ni, tile_ls, dls);
+    if (e != cudaSuccess) return c.cuda_fail(e, "instance log-sum");
+    c.stats.kernel_launches += 1;
+    if (out) {
+      out->d_logsum_sorted = dls;
+      out->slot_order = slot_order;
+    }
+  }
+  e = cudaMemcpyAsync(c.h_nsrc_d, dnsrc, sizeof(uint64_t) * 3, cudaMemcpyDeviceToHost, st);
+  if (e != cudaSuccess) return c.cuda_fail(e, "read pair count");
+  c.stats.instances += ni;
+  c.stats.tiles += n_slots;
+  c.pending_pairs = true;
+  return ENT_OK;
+}
+
+void Ctx::collect_kernel_stats() {
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, ev_k0, ev_k1) == cudaSuccess) stats.pair_kernel_ms = ms;
+  for (int d = 0; d < 3; ++d) {
+    if (ran_d[d] && cudaEventElapsedTime(&ms, ev_d[d][0], ev_d[d][1]) == cudaSuccess)
+      stats.pair_kernel_ms_by_dim[d] = ms;
+    ran_d[d] = false;
+    if (pending_pairs) {
+      stats.candidate_pairs_by_dim[d] = h_nsrc_d[d];
+      stats.candidate_pairs += h_nsrc_d[d];
+    }
+  }
+  cudaGetLastError();
+  pending_pairs = false;
+}
+
+// ------------------------------------------------------------------ C ABI
+extern "C" {
+
+int ent_create(ent_ctx** out, int device) {
+  if (!out) return ENT_ERR_ARG;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return ENT_ERR_NO_DEVICE;
+  }
+  if (device < 0) {
+    if (cudaGetDevice(&device) != cudaSuccess) return ENT_ERR_CUDA;
+  }
+  if (device >= n) return ENT_ERR_ARG;
+  Ctx* c = new Ctx();
+  c->device = device;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMalloc(&c->d_err, 16) != cudaSuccess ||
+      cudaEventCreate(&c->ev_call0) != cudaSuccess ||
+      cudaEventCreate(&c->ev_call1) != cudaSuccess ||
+      cudaEventCreate(&c->ev_k0) != cudaSuccess ||
+      cudaEventCreate(&c->ev_k1) != cudaSuccess ||
+      cudaEventCreate(&c->ev_d[0][0]) != cudaSuccess ||
+      cudaEventCreate(&c->ev_d[0][1]) != cudaSuccess ||
+      cudaEventCreate(&c->ev_d[1][0]) != cudaSuccess ||
+      cudaEventCreate(&c->ev_d[1][1]) != cudaSuccess ||
+      cudaEventCreate(&c->ev_d[2][0]) != cudaSuccess ||
+      cudaEventCreate(&c->ev_d[2][1]) != cudaSuccess ||
+      cudaDeviceGetAttribute(&c->n_sms, cudaDevAttrMultiProcessorCount, device) !=
+          cudaSuccess) {
+    cudaGetLastError();
+    delete c;
+    return ENT_ERR_CUDA;
+  }
+  *out = reinterpret_cast<ent_ctx*>(c);
+  return ENT_OK;
+}
+
+void ent_destroy(ent_ctx* ctx) {
+  if (!ctx) return;
+  Ctx* c = reinterpret_cast<Ctx*>(ctx);
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  c->arena.release();
+  cudaFree(c->d_err);
+  cudaEventDestroy(c->ev_call0);
+  cudaEventDestroy(c->ev_call1);
+  cudaEventDestroy(c->ev_k0);
+  cudaEventDestroy(c->ev_k1);
+  for (int d = 0; d < 3; ++d) {
+    cudaEventDestroy(c->ev_d[d][0]);
+    cudaEventDestroy(c->ev_d[d][1]);
+  }
+  cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char* ent_status_string(int s) {
+  switch (s) {
+    case ENT_OK: return "ok";
+    case ENT_ERR_DIM: return "can only compute combined probabilities in 1, 2 or 3 dimensions";
+    case ENT_ERR_H_COUNT: return "number of bandwidth parameters does not match number of selected columns";
+    case ENT_ERR_TAU_COUNT: return "number of lagtimes (tau) does not match number of selected dimensions";
+    case ENT_ERR_ARG: return "invalid argument";
+    case ENT_ERR_NONFINITE: return "non-finite coordinate";
+    case ENT_ERR_CUDA: return "CUDA error";
+    case ENT_ERR_NO_DEVICE: return "no CUDA-compatible GPUs found";
+    case ENT_ERR_TIMEOUT: return "device-side wait timed out";
+    case ENT_ERR_TOO_LARGE: return "input too large";
+    case ENT_ERR_STATE: return "invalid state";
+  }
+  return "unknown status";
+}
+
+const char* ent_last_error(const ent_ctx* ctx) {
+  if (!ctx) return "";
+  return reinterpret_cast<const Ctx*>(ctx)->last_error.c_str();
+}
+
+int ent_last_stats(const ent_ctx* ctx, ent_call_stats* s) {
+  if (!ctx || !s) return ENT_ERR_ARG;
+  *s = reinterpret_cast<const Ctx*>(ctx)->stats;
+  return ENT_OK;
+}
+
+}  // extern "C"
+
+// Validation shared by the density entry points (densities_common.hxx:7-49).
+int validate_selection(Ctx& c, size_t n_rows, size_t n_cols,
+                       const uint32_t* i_cols, const float* h,
+                       const uint32_t* tau, uint32_t d, size_t* n_sel) {
+  if (d < 1 || d > 3)
+    return c.fail(ENT_ERR_DIM, ent_status_string(ENT_ERR_DIM));
+  if (!i_cols || !h) return c.fail(ENT_ERR_ARG, "null column or bandwidth array");
+  uint32_t tmax = 0;
+  for (uint32_t j = 0; j < d; ++j) {
+    if (i_cols[j] >= n_cols) return c.fail(ENT_ERR_ARG, "column index out of range");
+    if (!(h[j] > 0.f) || !std::isfinite(h[j]))
+      return c.fail(ENT_ERR_ARG, "bandwidth must be finite and positive");
+    if (tau) tmax = std::max(tmax, tau[j]);
+  }
+  if ((size_t)tmax >= n_rows) return c.fail(ENT_ERR_ARG, "lag not smaller than n_rows");
+  if (n_rows > 0xffffff00ull) return c.fail(ENT_ERR_TOO_LARGE, "too many rows");
+  *n_sel = n_rows - tmax;
+  return ENT_OK;
+}
+
+static int densities_impl(ent_ctx* ctx, const float* coords, size_t n_rows,
+                          size_t n_cols, const uint32_t* i_cols, const float* h,
+                          const uint32_t* tau, uint32_t d, uint32_t flags,
+                          double* out, size_t* n_out, bool device_io,
+                          bool counts) {
+  if (!ctx) return ENT_ERR_ARG;
+  Ctx& c = *reinterpret_cast<Ctx*>(ctx);
+  int s = c.begin_call();
+  if (s) return s;
+  size_t n_sel = 0;
+  s = validate_selection(c, n_rows, n_cols, i_cols, h, tau, d, &n_sel);
+  if (s) return s;
+  if (n_out) *n_out = n_sel;
+  if (!coords || !out) return c.fail(ENT_ERR_ARG, "null coords or output");
+  cudaError_t e;
+  std::vector<ViewSpec> views(d);
+  for (uint32_t j = 0; j < d; ++j) {
+    const size_t off = (size_t)i_cols[j] * n_rows + (tau ? tau[j] : 0);
+    if (device_io) {
+      views[j].x = coords + off;
+    } else {
+      float* p = static_cast<float*>(c.arena.alloc(4 * n_sel));
+      if (!p) return c.fail(ENT_ERR_CUDA, "out of device memory");
+      e = cudaMemcpyAsync(p, coords + off, 4 * n_sel, cudaMemcpyHostToDevice, c.stream);
+      if (e != cudaSuccess) return c.cuda_fail(e, "copy coordinates");
+      views[j].x = p;
+    }
+    views[j].n = (uint32_t)n_sel;
+  }
+  double* dout = out;
+  if (!device_io) {
+    dout = static_cast<double*>(c.arena.alloc(8 * n_sel));
+    if (!dout) return c.fail(ENT_ERR_CUDA, "out of device memory");
+  }
+  std::vector<InstSpec> insts(1);
+  InstSpec& I = insts[0];
+  I.d = d;
+  I.n = (uint32_t)n_sel;
+  for (uint32_t j = 0; j < d; ++j) {
+    I.view[j] = j;
+    I.h[j] = h[j];
+  }
+  I.norm = counts ? 1.0 : ((flags & ENT_COMPAT_NORM) ? (double)n_rows : (double)n_sel);
+  I.out = dout;
+  I.S = c.strip_subdiv;
+  Engine eng;
+  s = eng.run(c, views, insts, DM_WRITE_F64 | (counts ? DM_COUNT : 0u), nullptr);
+  if (s) return s;
+  if (!device_io) {
+    e = cudaMemcpyAsync(out, dout, 8 * n_sel, cudaMemcpyDeviceToHost, c.stream);
+    if (e != cudaSuccess) return c.cuda_fail(e, "copy densities");
+  }
+  s = c.end_call();
+  c.collect_kernel_stats();
+  return s;
+}
+
+extern "C" {
+
+int ent_densities(ent_ctx* ctx, const float* coords, size_t n_rows,
+                  size_t n_cols, const uint32_t* i_cols, const float* h,
+                  const uint32_t* tau, uint32_t d, uint32_t flags, double* out,
+                  size_t* n_out) {
+  return densities_impl(ctx, coords, n_rows, n_cols, i_cols, h, tau, d, flags,
+                        out, n_out, false, false);
+}
+
+int ent_densities_device(ent_ctx* ctx, const float* d_coords, size_t n_rows,
+                         size_t n_cols, const uint32_t* i_cols, const float* h,
+                         const uint32_t* tau, uint32_t d, uint32_t flags,
+                         double* d_out, size_t* n_out) {
+  return densities_impl(ctx, d_coords, n_rows, n_cols, i_cols, h, tau, d, flags,
+                        d_out, n_out, true, false);
+}
+
+int ent_support_counts(ent_ctx* ctx, const float* coords, size_t n_rows,
+                       size_t n_cols, const uint32_t* i_cols, const float* h,
+                       const uint32_t* tau, uint32_t d, double* out,
+                       size_t* n_out) {
+  return densities_impl(ctx, coords, n_rows, n_cols, i_cols, h, tau, d, 0u, out,
+                        n_out, false, true);
+}
+
+}  // extern "C"

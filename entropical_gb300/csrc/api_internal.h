@@ -1,0 +1,81 @@
+// Host-side context, workspace and batch engine shared by the C ABI files.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/entropical_gb300.h"
+
+// Grow-only device workspace. Blocks are kept across calls; when a call
+// needed more than one block, the next call coalesces them into one.
+struct Arena {
+  struct Block {
+    void* ptr;
+    size_t size;
+  };
+  std::vector<Block> blocks;
+  size_t used_in_last = 0;
+  size_t total_used = 0;
+  void* alloc(size_t bytes);
+  void reset();
+  void release();
+};
+
+struct Ctx {
+  int device = 0;
+  int n_sms = 1;
+  cudaStream_t stream = nullptr;
+  uint32_t* d_err = nullptr;
+  cudaEvent_t ev_call0 = nullptr, ev_call1 = nullptr;
+  cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr;
+  cudaEvent_t ev_d[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
+  bool ran_d[3] = {false, false, false};
+  uint64_t h_nsrc_d[3] = {0, 0, 0};
+  Arena arena;
+  std::string last_error;
+  ent_call_stats stats{};
+  bool pending_pairs = false;
+  uint32_t strip_subdiv = 2;  // cells per bandwidth along dimension 1 (d = 2)
+
+  int fail(int status, const std::string& msg);
+  int cuda_fail(cudaError_t e, const char* where);
+  int begin_call();
+  int end_call();
+  void collect_kernel_stats();
+};
+
+// A device column view of n float32 values.
+struct ViewSpec {
+  const float* x;
+  uint32_t n;
+};
+
+// One density instance over d views.
+struct InstSpec {
+  uint32_t d = 1;
+  uint32_t n = 0;
+  uint32_t view[3] = {0, 0, 0};
+  float h[3] = {1.f, 1.f, 1.f};
+  double norm = 1.0;
+  double* out = nullptr;  // device, by original index (nullable)
+  uint32_t S = 2;
+};
+
+struct EngineOut {
+  double* d_logsum_sorted = nullptr;  // per instance, in slot order
+  std::vector<uint32_t> slot_order;   // slot rank -> instance index
+};
+
+struct Engine {
+  uint32_t group_base[4] = {0, 0, 0, 0};
+  uint32_t group_slots[4] = {0, 0, 0, 0};
+  int run(Ctx& c, const std::vector<ViewSpec>& views,
+          std::vector<InstSpec>& insts, uint32_t mode, EngineOut* out);
+};
+
+int validate_selection(Ctx& c, size_t n_rows, size_t n_cols,
+                       const uint32_t* i_cols, const float* h,
+                       const uint32_t* tau, uint32_t d, size_t* n_sel);

@@ -1,0 +1,812 @@
+// Product-Epanechnikov density sums on device-built cell lists (sm_103a).
+//
+// Replaces the reference density backends: the dense all-pairs CUDA kernels
+// density_{1,2,3}d_krnl (density_1d.cuh:51-90, density_2d.cuh:57-100,
+// density_3d.cuh:61-108) and the OpenMP window loops
+// (densities_omp.cpp:33-159). For every target point t
+//     S_t = sum_s prod_j max(0, 1 - (y_tj - y_sj)^2),   y = (x - c)/h,
+//     p_t = 0.75^d / (norm * prod_j h_j) * S_t,
+// which equals the reference's sum of 0.75 (1-u^2)/h products.
+//
+// Cell lists ("strips"): points are sorted on dimension 0; dimensions 1..d-1
+// are binned into cells of width h/S, and a stable partition by cell keeps
+// dimension-0 order inside each strip. A target tile (up to TT consecutive
+// points of one strip) then sees all of its in-support sources inside
+// (2S+1)^(d-1) contiguous runs: one per neighbouring strip, clipped by
+// binary search to [y0_first - 1, y0_last + 1]. This is the device form of
+// the reference's sorted-window search boxes() (densities_omp.cpp:33-65) and
+// of the cell boxes of Transs::BoxedSearch (boxedsearch.cpp:15-62).
+//
+// The pair kernel is a persistent CTA loop over an atomic work queue of
+// tiles. Source runs are staged into shared memory in double-buffered chunks
+// with cp.async.bulk (TMA bulk copies) completing on mbarriers; four warps
+// each own R register-resident targets and stride the chunk with their 32
+// lanes. The pair body is branchless FP32 on the CUDA cores using packed
+// f32x2 sub/fma: for d = 2 one pair is sub.f32x2, fma.f32x2, 2 min, 1 fma.
+// Per-lane chunk partials are folded into Kahan-compensated FP32 sums; the
+// per-point scale, log and entropy sums are FP64.
+#include <cfloat>
+
+#include "engine.h"
+
+namespace ent {
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+// ------------------------------------------------------------ column stats
+__global__ void __launch_bounds__(1024)
+    k_colstats(const ViewDev* __restrict__ views, ViewStats* __restrict__ stats) {
+  __shared__ float smn[32], smx[32];
+  __shared__ double ss1[32], ss2[32];
+  __shared__ uint32_t sbad[32];
+  const ViewDev v = views[blockIdx.x];
+  float mn = FLT_MAX, mx = -FLT_MAX;
+  double s1 = 0.0, s2 = 0.0;
+  uint32_t bad = 0;
+  for (uint32_t i = threadIdx.x; i < v.n; i += blockDim.x) {
+    const float f = v.x[i];
+    if (!isfinite(f)) {
+      bad = 1;
+      continue;
+    }
+    mn = fminf(mn, f);
+    mx = fmaxf(mx, f);
+    s1 += (double)f;
+    s2 += (double)f * (double)f;
+  }
+  for (int o = 16; o; o >>= 1) {
+    mn = fminf(mn, __shfl_xor_sync(FULL, mn, o));
+    mx = fmaxf(mx, __shfl_xor_sync(FULL, mx, o));
+    s1 += __shfl_xor_sync(FULL, s1, o);
+    s2 += __shfl_xor_sync(FULL, s2, o);
+    bad |= __shfl_xor_sync(FULL, bad, o);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    smn[warp] = mn;
+    smx[warp] = mx;
+    ss1[warp] = s1;
+    ss2[warp] = s2;
+    sbad[warp] = bad;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+    mn = lane < nw ? smn[lane] : FLT_MAX;
+    mx = lane < nw ? smx[lane] : -FLT_MAX;
+    s1 = lane < nw ? ss1[lane] : 0.0;
+    s2 = lane < nw ? ss2[lane] : 0.0;
+    bad = lane < nw ? sbad[lane] : 0u;
+    for (int o = 16; o; o >>= 1) {
+      mn = fminf(mn, __shfl_xor_sync(FULL, mn, o));
+      mx = fmaxf(mx, __shfl_xor_sync(FULL, mx, o));
+      s1 += __shfl_xor_sync(FULL, s1, o);
+      s2 += __shfl_xor_sync(FULL, s2, o);
+      bad |= __shfl_xor_sync(FULL, bad, o);
+    }
+    if (lane == 0) {
+      ViewStats r;
+      r.mn = mn;
+      r.mx = mx;
+      r.s1 = s1;
+      r.s2 = s2;
+      r.nonfinite = bad;
+      r.pad = 0;
+      stats[blockIdx.x] = r;
+    }
+  }
+}
+
+// ---------------------------------------------------------- sort keys
+__global__ void k_view_keys(const ViewDev* __restrict__ views,
+                            const uint64_t* __restrict__ view_off,
+                            uint32_t* __restrict__ keys,
+                            uint32_t* __restrict__ vals) {
+  const ViewDev v = views[blockIdx.y];
+  const uint64_t base = view_off[blockIdx.y];
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < v.n;
+       i += gridDim.x * blockDim.x) {
+    keys[base + i] = float_key(v.x[i]);
+    vals[base + i] = i;
+  }
+}
+
+__device__ __forceinline__ uint32_t cell_of(float x, float lo, double inv_w,
+                                            uint32_t ncell) {
+  const double a = ((double)x - (double)lo) * inv_w;
+  int64_t c = (int64_t)floor(a);
+  if (c < 0) c = 0;
+  if (c >= (int64_t)ncell) c = ncell - 1;
+  return (uint32_t)c;
+}
+
+__global__ void k_strip_keys(const InstDev* __restrict__ insts,
+                             const uint32_t* __restrict__ inst_ids,
+                             const uint64_t* __restrict__ seg_off,
+                             uint32_t* __restrict__ keys,
+                             uint32_t* __restrict__ vals) {
+  const InstDev& I = insts[inst_ids[blockIdx.y]];
+  const uint64_t base = seg_off[blockIdx.y];
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < I.n;
+       k += gridDim.x * blockDim.x) {
+    const uint32_t j = I.perm0[k];
+    uint32_t key = cell_of(I.x[1][j], I.lo1, I.inv_w1, I.ncell1);
+    if (I.d == 3) key = key * I.ncell2 + cell_of(I.x[2][j], I.lo2, I.inv_w2, I.ncell2);
+    keys[base + k] = key;
+    vals[base + k] = j;
+  }
+}
+
+__global__ void k_strip_bounds(const InstDev* __restrict__ insts) {
+  const InstDev& I = insts[blockIdx.y];
+  const uint32_t n = I.n;
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k <= n;
+       k += gridDim.x * blockDim.x) {
+    if (I.d == 1) {
+      if (k == 0) I.strip_start[0] = 0;
+      if (k == n) I.strip_start[1] = n;
+      continue;
+    }
+    const int64_t prev = (k == 0) ? -1 : (int64_t)I.skeys[k - 1];
+    const int64_t cur = (k == n) ? (int64_t)I.n_strips : (int64_t)I.skeys[k];
+    for (int64_t s = prev + 1; s <= cur; ++s) I.strip_start[s] = k;
+  }
+}
+
+// Exclusive scan of tiles-per-strip, one block per instance.
+__global__ void __launch_bounds__(1024) k_tile_offsets(const InstDev* __restrict__ insts) {
+  __shared__ uint32_t warp_tot[32];
+  __shared__ uint32_t carry_s;
+  const InstDev& I = insts[blockIdx.x];
+  const uint32_t L = I.n_strips;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) carry_s = 0;
+  __syncthreads();
+  for (uint32_t base = 0; base < L; base += 1024) {
+    const uint32_t i = base + threadIdx.x;
+    uint32_t v = 0;
+    if (i < L) {
+      const uint32_t len = I.strip_start[i + 1] - I.strip_start[i];
+      v = (len + I.tt - 1) / I.tt;
+    }
+    uint32_t x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(FULL, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      uint32_t w = warp_tot[lane];
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(FULL, w, o);
+        if (lane >= o) w += y;
+      }
+      warp_tot[lane] = w;
+    }
+    __syncthreads();
+    const uint32_t carry = carry_s;
+    if (i < L) I.tile_off[i] = carry + (warp ? warp_tot[warp - 1] : 0u) + x - v;
+    __syncthreads();
+    if (threadIdx.x == 0) carry_s = carry + warp_tot[31];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) I.tile_off[L] = carry_s;
+}
+
+__global__ void k_gather_pts(const InstDev* __restrict__ insts) {
+  const InstDev& I = insts[blockIdx.y];
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < I.n;
+       k += gridDim.x * blockDim.x) {
+    const uint32_t j = I.perm[k];
+    const float y0 = __fmul_rn(__fsub_rn(I.x[0][j], I.center[0]), I.inv_h[0]);
+    if (I.d == 1) {
+      reinterpret_cast<float*>(I.pts)[k] = y0;
+    } else if (I.d == 2) {
+      const float y1 = __fmul_rn(__fsub_rn(I.x[1][j], I.center[1]), I.inv_h[1]);
+      reinterpret_cast<float2*>(I.pts)[k] = make_float2(y0, y1);
+    } else {
+      const float y1 = __fmul_rn(__fsub_rn(I.x[1][j], I.center[1]), I.inv_h[1]);
+      const float y2 = __fmul_rn(__fsub_rn(I.x[2][j], I.center[2]), I.inv_h[2]);
+      reinterpret_cast<float4*>(I.pts)[k] = make_float4(y0, y1, y2, 0.f);
+    }
+  }
+}
+
+// ------------------------------------------------------------- tile plan
+__device__ __forceinline__ float y0_at(const void* pts, int d, uint32_t k) {
+  if (d == 1) return reinterpret_cast<const float*>(pts)[k];
+  if (d == 2) return reinterpret_cast<const float2*>(pts)[k].x;
+  return reinterpret_cast<const float4*>(pts)[k].x;
+}
+
+// first k in [a, b) with y0(k) >= v
+__device__ uint32_t lower_y(const void* pts, int d, uint32_t a, uint32_t b, float v) {
+  while (a < b) {
+    const uint32_t m = a + (b - a) / 2;
+    if (y0_at(pts, d, m) < v) a = m + 1; else b = m;
+  }
+  return a;
+}
+// first k in [a, b) with y0(k) > v
+__device__ uint32_t upper_y(const void* pts, int d, uint32_t a, uint32_t b, float v) {
+  while (a < b) {
+    const uint32_t m = a + (b - a) / 2;
+    if (y0_at(pts, d, m) <= v) a = m + 1; else b = m;
+  }
+  return a;
+}
+
+__global__ void k_plan(const InstDev* __restrict__ insts, uint32_t n_inst,
+                       const uint32_t* __restrict__ inst_tile_base,
+                       TileDesc* __restrict__ tiles, uint32_t n_slots,
+                       unsigned long long* __restrict__ n_src_total) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n_slots) return;
+  uint32_t lo = 0, hi = n_inst;
+  while (hi - lo > 1) {
+    const uint32_t m = (lo + hi) / 2;
+    if (inst_tile_base[m] <= g) lo = m; else hi = m;
+  }
+  const InstDev& I = insts[lo];
+  TileDesc td;
+  td.inst = lo;
+  td.t_begin = 0;
+  td.t_count = 0;
+  td.n_runs = 0;
+  const uint32_t t = g - I.tile_base;
+  const uint32_t total = I.tile_off[I.n_strips];
+  if (t >= total) {
+    tiles[g] = td;
+    return;
+  }
+  uint32_t a = 0, b = I.n_strips;
+  while (b - a > 1) {
+    const uint32_t m = (a + b) / 2;
+    if (I.tile_off[m] <= t) a = m; else b = m;
+  }
+  const uint32_t s = a;
+  const int d = (int)I.d;
+  const uint32_t tb = I.strip_start[s] + (t - I.tile_off[s]) * I.tt;
+  const uint32_t tc = min(I.tt, I.strip_start[s + 1] - tb);
+  const float yf = y0_at(I.pts, d, tb);
+  const float yl = y0_at(I.pts, d, tb + tc - 1);
+  const float eps = 1e-5f * (1.f + fmaxf(fabsf(yf), fabsf(yl)));
+  const float vlo = yf - 1.f - eps, vhi = yl + 1.f + eps;
+  td.t_begin = tb;
+  td.t_count = tc;
+  uint32_t nr = 0;
+  unsigned long long nsrc = 0;
+  auto add_strip = [&](uint32_t sp) {
+    const uint32_t a0 = I.strip_start[sp], b0 = I.strip_start[sp + 1];
+    if (a0 == b0) return;
+    const uint32_t l = lower_y(I.pts, d, a0, b0, vlo);
+    const uint32_t h = upper_y(I.pts, d, l, b0, vhi);
+    if (h <= l) return;
+    if (nr > 0 && td.lo[nr - 1] + td.len[nr - 1] == l) {
+      td.len[nr - 1] += h - l;
+    } else {
+      td.lo[nr] = l;
+      td.len[nr] = h - l;
+      ++nr;
+    }
+    nsrc += h - l;
+  };
+  if (d == 1) {
+    add_strip(0);
+  } else if (d == 2) {
+    const int S = (int)I.S;
+    const int c1 = (int)s;
+    for (int c = max(0, c1 - S); c <= min((int)I.ncell1 - 1, c1 + S); ++c)
+      add_strip((uint32_t)c);
+  } else {
+    const int c1 = (int)(s / I.ncell2), c2 = (int)(s % I.ncell2);
+    for (int u = max(0, c1 - 1); u <= min((int)I.ncell1 - 1, c1 + 1); ++u)
+      for (int v = max(0, c2 - 1); v <= min((int)I.ncell2 - 1, c2 + 1); ++v)
+        add_strip((uint32_t)u * I.ncell2 + (uint32_t)v);
+  }
+  td.n_runs = nr;
+  tiles[g] = td;
+  if (n_src_total) atomicAdd(n_src_total + (d - 1), nsrc * (unsigned long long)tc);
+}
+
+// ------------------------------------------------------- pair kernel
+template <int D> struct PtType;
+template <> struct PtType<1> { typedef float T; };
+template <> struct PtType<2> { typedef float2 T; };
+template <> struct PtType<3> { typedef float4 T; };
+
+template <int D, int R>
+struct Cfg {
+  static constexpr int NW = 4;
+  static constexpr int NT = NW * 32;
+  static constexpr int TT = NW * R;
+  typedef typename PtType<D>::T P;
+  static constexpr int E = sizeof(P);
+  static constexpr int A = 16 / E;  // 16-byte alignment, in elements
+  static constexpr int CH = (D == 1) ? 4096 : (D == 2 ? 2048 : 1024);
+  static constexpr int MAXP = MAX_RUNS + 1;
+  static constexpr int CAP = CH + 2 * A * MAXP;
+  static constexpr size_t SMEM = 2 * (size_t)CAP * E;
+};
+
+struct Piece {
+  uint32_t s0;   // shared-memory element index of the first exact element
+  uint32_t n;    // exact elements
+  uint32_t g0;   // first copied element (16-byte aligned) in the points array
+  uint32_t cnt;  // copied elements
+  uint32_t o;    // shared-memory element offset of the copy
+};
+
+template <int D, int R>
+__device__ __forceinline__ void issue_chunk(
+    uint32_t c, uint32_t b, uint32_t nsrc, uint32_t nr, const uint32_t* run_lo,
+    const uint32_t* run_pre, const typename Cfg<D, R>::P* pts,
+    typename Cfg<D, R>::P* bufs, Piece (*ptab)[Cfg<D, R>::MAXP], uint32_t* npc,
+    uint64_t* full) {
+  typedef Cfg<D, R> C;
+  const uint32_t begin = c * C::CH;
+  const uint32_t end = min(begin + (uint32_t)C::CH, nsrc);
+  uint32_t np = 0, o = 0, bytes = 0;
+  for (uint32_t r = 0; r < nr; ++r) {
+    const uint32_t rb = run_pre[r], re = run_pre[r + 1];
+    if (re <= begin || rb >= end) continue;
+    const uint32_t a = run_lo[r] + (max(begin, rb) - rb);
+    const uint32_t e = run_lo[r] + (min(end, re) - rb);
+    const uint32_t a0 = a & ~(uint32_t)(C::A - 1);
+    const uint32_t e0 = (e + C::A - 1) & ~(uint32_t)(C::A - 1);
+    Piece p;
+    p.s0 = o + (a - a0);
+    p.n = e - a;
+    p.g0 = a0;
+    p.cnt = e0 - a0;
+    p.o = o;
+    ptab[b][np++] = p;
+    o += e0 - a0;
+    bytes += (e0 - a0) * C::E;
+  }
+  npc[b] = np;
+  fence_proxy_async_smem();
+  mbar_arrive_expect_tx(&full[b], bytes);
+  typename C::P* dst = bufs + (size_t)b * C::CAP;
+  for (uint32_t i = 0; i < np; ++i) {
+    const Piece p = ptab[b][i];
+    bulk_g2s(dst + p.o, pts + p.g0, p.cnt * C::E, &full[b]);
+  }
+}
+
+// Sum v[0..R) over the 32 lanes so that lane l ends with the total of
+// target (l >> (5 - log2 R)); 2R-2 + (5 - log2 R) shuffles.
+template <int R>
+__device__ __forceinline__ float warp_transpose_sum(float (&v)[R], int lane) {
+#pragma unroll
+  for (int cnt = R, mask = 16; cnt > 1; cnt >>= 1, mask >>= 1) {
+    const bool up = (lane & mask) != 0;
+#pragma unroll
+    for (int i = 0; i < cnt / 2; ++i) {
+      const float send = up ? v[i] : v[i + cnt / 2];
+      const float keep = up ? v[i + cnt / 2] : v[i];
+      v[i] = keep + __shfl_xor_sync(FULL, send, mask);
+    }
+  }
+  float x = v[0];
+#pragma unroll
+  for (int mask = 32 / R / 2; mask >= 1; mask >>= 1)
+    x += __shfl_xor_sync(FULL, x, mask);
+  return x;
+}
+
+template <int R>
+struct Log2 {
+  static constexpr int v = (R <= 1) ? 0 : 1 + Log2<R / 2>::v;
+};
+template <>
+struct Log2<1> {
+  static constexpr int v = 0;
+};
+
+template <int D, int R>
+__global__ void __launch_bounds__(128)
+    k_density(const TileDesc* __restrict__ tiles, uint32_t n_slots,
+              const InstDev* __restrict__ insts, uint32_t* work_counter,
+              uint32_t* err, double* tile_logsum, uint32_t mode) {
+  typedef Cfg<D, R> C;
+  typedef typename C::P P;
+  extern __shared__ __align__(128) unsigned char dsm[];
+  P* bufs = reinterpret_cast<P*>(dsm);
+  __shared__ __align__(8) uint64_t full[2];
+  __shared__ Piece ptab[2][C::MAXP];
+  __shared__ uint32_t npc[2];
+  __shared__ uint32_t run_lo[MAX_RUNS], run_pre[MAX_RUNS + 1];
+  __shared__ uint32_t s_g, s_nr, s_tb, s_tc, s_inst;
+  __shared__ double s_lsum[C::NW];
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) {
+    mbar_init(&full[0], 1);
+    mbar_init(&full[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  const f32x2 M1 = pk2(-1.f, -1.f);
+  uint32_t q = 0;
+
+  for (;;) {
+    if (tid == 0) {
+      const uint32_t g = atomicAdd(work_counter, 1u);
+      s_g = g;
+      if (g < n_slots) {
+        const TileDesc* T = tiles + g;
+        const uint32_t nr = T->n_runs;
+        s_tb = T->t_begin;
+        s_tc = T->t_count;
+        s_inst = T->inst;
+        s_nr = nr;
+        run_pre[0] = 0;
+        for (uint32_t r = 0; r < nr; ++r) {
+          run_lo[r] = T->lo[r];
+          run_pre[r + 1] = run_pre[r] + T->len[r];
+        }
+      }
+    }
+    __syncthreads();
+    const uint32_t g = s_g;
+    if (g >= n_slots) break;
+    const uint32_t tc = s_tc;
+    if (tc == 0) {
+      if (tid == 0 && (mode & (DM_LOGSUM | DM_SUMV))) tile_logsum[g] = 0.0;
+      __syncthreads();
+      continue;
+    }
+    const InstDev* I = insts + s_inst;
+    const P* __restrict__ pts = reinterpret_cast<const P*>(I->pts);
+    const uint32_t nr = s_nr, nsrc = run_pre[nr], tb = s_tb;
+    const uint32_t nch = (nsrc + C::CH - 1) / C::CH;
+    if (tid == 0 && nch > 0)
+      issue_chunk<D, R>(0, q & 1u, nsrc, nr, run_lo, run_pre, pts, bufs, ptab,
+                        npc, full);
+
+    // Register-resident targets of this warp; missing ones sit far away.
+    float ks[R], kc[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      ks[r] = 0.f;
+      kc[r] = 0.f;
+    }
+    constexpr float FAR = 1e18f;
+    f32x2 T01[R];
+    float T2[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const uint32_t li = warp * R + r;
+      P p;
+      if (li < tc) {
+        p = pts[tb + li];
+      } else {
+        if constexpr (D == 1) p = FAR;
+        else if constexpr (D == 2) p = make_float2(FAR, FAR);
+        else p = make_float4(FAR, FAR, FAR, 0.f);
+      }
+      if constexpr (D == 1) {
+        T2[r] = p;
+      } else if constexpr (D == 2) {
+        T01[r] = pk2(p.x, p.y);
+      } else {
+        T01[r] = pk2(p.x, p.y);
+        T2[r] = p.z;
+      }
+    }
+
+    bool aborted = false;
+    uint32_t ab_q = 0;
+    bool ab_next = false;
+    for (uint32_t c = 0; c < nch; ++c) {
+      const uint32_t qq = q + c, b = qq & 1u;
+      if (tid == 0 && c + 1 < nch)
+        issue_chunk<D, R>(c + 1, (qq + 1) & 1u, nsrc, nr, run_lo, run_pre, pts,
+                          bufs, ptab, npc, full);
+      const bool ok = mbar_wait(&full[b], (qq >> 1) & 1u);
+      if (ok) {
+        const P* B = bufs + (size_t)b * C::CAP;
+        const uint32_t np = npc[b];
+        for (uint32_t pi = 0; pi < np; ++pi) {
+          const uint32_t s0 = ptab[b][pi].s0, n = ptab[b][pi].n;
+          if (mode & DM_COUNT) {
+            // Same support test as the sum loops: fma(d, d, -1) <= 0 per dim.
+            float acc[R];
+#pragma unroll
+            for (int r = 0; r < R; ++r) acc[r] = 0.f;
+            for (uint32_t k = lane; k < n; k += 32) {
+              const P s = B[s0 + k];
+#pragma unroll
+              for (int r = 0; r < R; ++r) {
+                bool in;
+                if constexpr (D == 1) {
+                  const float dd = __fsub_rn(T2[r], s);
+                  in = fmaf(dd, dd, -1.f) <= 0.f;
+                } else {
+                  float tx, ty;
+                  upk2(T01[r], tx, ty);
+                  const float dx = __fsub_rn(tx, s.x), dy = __fsub_rn(ty, s.y);
+                  in = fmaf(dx, dx, -1.f) <= 0.f && fmaf(dy, dy, -1.f) <= 0.f;
+                  if constexpr (D == 3) {
+                    const float dz = __fsub_rn(T2[r], s.z);
+                    in = in && fmaf(dz, dz, -1.f) <= 0.f;
+                  }
+                }
+                acc[r] += in ? 1.f : 0.f;
+              }
+            }
+#pragma unroll
+            for (int r = 0; r < R; ++r) kahan_add(ks[r], kc[r], acc[r]);
+          } else if constexpr (D == 1) {
+            f32x2 acc[R / 2];
+            f32x2 T[R / 2];
+#pragma unroll
+            for (int i = 0; i < R / 2; ++i) {
+              acc[i] = pk2(0.f, 0.f);
+              T[i] = pk2(T2[2 * i], T2[2 * i + 1]);
+            }
+#pragma unroll 2
+            for (uint32_t k = lane; k < n; k += 32) {
+              const float s = B[s0 + k];
+              const f32x2 S = pk2(s, s);
+#pragma unroll
+              for (int i = 0; i < R / 2; ++i) {
+                const f32x2 dd = sub2(T[i], S);
+                const f32x2 v = fma2(dd, dd, M1);
+                float va, vb;
+                upk2(v, va, vb);
+                acc[i] = add2(acc[i], pk2(fminf(va, 0.f), fminf(vb, 0.f)));
+              }
+            }
+#pragma unroll
+            for (int i = 0; i < R / 2; ++i) {
+              float a0, a1;
+              upk2(acc[i], a0, a1);
+              kahan_add(ks[2 * i], kc[2 * i], -a0);
+              kahan_add(ks[2 * i + 1], kc[2 * i + 1], -a1);
+            }
+          } else if constexpr (D == 2) {
+            float acc[R];
+#pragma unroll
+            for (int r = 0; r < R; ++r) acc[r] = 0.f;
+#pragma unroll 2
+            for (uint32_t k = lane; k < n; k += 32) {
+              const float2 s = B[s0 + k];
+              const f32x2 S = pk2(s.x, s.y);
+#pragma unroll
+              for (int r = 0; r < R; ++r) {
+                const f32x2 dd = sub2(T01[r], S);
+                const f32x2 v = fma2(dd, dd, M1);
+                float vx, vy;
+                upk2(v, vx, vy);
+                acc[r] = fmaf(fminf(vx, 0.f), fminf(vy, 0.f), acc[r]);
+              }
+            }
+#pragma unroll
+            for (int r = 0; r < R; ++r) kahan_add(ks[r], kc[r], acc[r]);
+          } else {
+            float acc[R];
+#pragma unroll
+            for (int r = 0; r < R; ++r) acc[r] = 0.f;
+#pragma unroll 2
+            for (uint32_t k = lane; k < n; k += 32) {
+              const float4 s = B[s0 + k];
+              const f32x2 S = pk2(s.x, s.y);
+#pragma unroll
+              for (int r = 0; r < R; ++r) {
+                const f32x2 dd = sub2(T01[r], S);
+                const float dz = T2[r] - s.z;
+                const f32x2 v = fma2(dd, dd, M1);
+                const float vz = fmaf(dz, dz, -1.f);
+                float vx, vy;
+                upk2(v, vx, vy);
+                const float pxy = fminf(vx, 0.f) * fminf(vy, 0.f);
+                acc[r] = fmaf(pxy, fminf(vz, 0.f), acc[r]);
+              }
+            }
+#pragma unroll
+            for (int r = 0; r < R; ++r) kahan_add(ks[r], kc[r], -acc[r]);
+          }
+        }
+      }
+      if (__syncthreads_or(!ok)) {
+        aborted = true;
+        ab_q = qq;
+        ab_next = c + 1 < nch;
+        break;
+      }
+    }
+    if (aborted) {
+      // Let any copy still in flight land before this CTA's shared memory
+      // is released, then report and stop.
+      if (tid == 0) {
+        atomicOr(err, EF_TIMEOUT);
+        mbar_wait(&full[ab_q & 1u], (ab_q >> 1) & 1u);
+        if (ab_next) mbar_wait(&full[(ab_q + 1) & 1u], ((ab_q + 1) >> 1) & 1u);
+      }
+      __syncthreads();
+      return;
+    }
+    q += nch;
+
+    // Epilogue: combine lanes, scale in FP64, write / log-sum.
+    float v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = ks[r] - kc[r];
+    const float tot = warp_transpose_sum<R>(v, lane);
+    const int tgt = lane >> (5 - Log2<R>::v);
+    const bool writer = (lane & ((32 / R) - 1)) == 0;
+    const uint32_t li = warp * R + tgt;
+    double lsum = 0.0;
+    if (writer && li < tc) {
+      const double dens = I->scale * (double)tot;
+      if (mode & DM_WRITE_F64) I->out[I->perm[tb + li]] = dens;
+      if (mode & DM_LOGSUM) lsum = log(dens);
+      else if (mode & DM_SUMV) lsum = dens;
+    }
+    if (mode & (DM_LOGSUM | DM_SUMV)) {
+      for (int o = 16; o; o >>= 1) lsum += __shfl_xor_sync(FULL, lsum, o);
+      if (lane == 0) s_lsum[warp] = lsum;
+    }
+    __syncthreads();
+    if (tid == 0 && (mode & (DM_LOGSUM | DM_SUMV))) {
+      double t = 0.0;
+#pragma unroll
+      for (int w = 0; w < C::NW; ++w) t += s_lsum[w];
+      tile_logsum[g] = t;
+    }
+  }
+}
+
+template <int D, int R>
+cudaError_t launch_density_t(cudaStream_t st, const TileDesc* tiles,
+                             uint32_t n_slots, const InstDev* insts,
+                             uint32_t* work_counter, uint32_t* err,
+                             double* tile_logsum, uint32_t mode, int n_sms,
+                             int* launched) {
+  typedef Cfg<D, R> C;
+  auto kern = k_density<D, R>;
+  cudaError_t e = cudaFuncSetAttribute(
+      kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, C::NT,
+                                                    C::SMEM);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  uint64_t grid = (uint64_t)per_sm * (uint64_t)n_sms;
+  if (grid > n_slots) grid = n_slots;
+  if (grid == 0) grid = 1;
+  e = cudaMemsetAsync(work_counter, 0, sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
+  kern<<<(unsigned)grid, C::NT, C::SMEM, st>>>(tiles, n_slots, insts,
+                                               work_counter, err, tile_logsum,
+                                               mode);
+  if (launched) *launched = (int)grid;
+  return cudaGetLastError();
+}
+
+// Deterministic per-instance sum of the tile log-sums.
+__global__ void __launch_bounds__(256)
+    k_inst_logsum(const InstDev* __restrict__ insts,
+                  const double* __restrict__ tile_logsum, double* out) {
+  __shared__ double sw[8];
+  const InstDev& I = insts[blockIdx.x];
+  const uint32_t n = I.tile_cap;
+  double a = 0.0;
+  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+    a += tile_logsum[I.tile_base + i];
+  for (int o = 16; o; o >>= 1) a += __shfl_xor_sync(FULL, a, o);
+  if ((threadIdx.x & 31) == 0) sw[threadIdx.x >> 5] = a;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < 8; ++w) t += sw[w];
+    out[blockIdx.x] = t;
+  }
+}
+
+}  // namespace
+
+// Targets per warp for each dimension (tile = 4 warps).
+constexpr int R1 = 16, R2 = 16, R3 = 8;
+
+int density_tile_targets(int d) {
+  return d == 1 ? Cfg<1, R1>::TT : (d == 2 ? Cfg<2, R2>::TT : Cfg<3, R3>::TT);
+}
+
+cudaError_t launch_colstats(cudaStream_t st, const ViewDev* views,
+                            uint32_t n_views, ViewStats* stats) {
+  if (n_views == 0) return cudaSuccess;
+  k_colstats<<<n_views, 1024, 0, st>>>(views, stats);
+  return cudaGetLastError();
+}
+
+static unsigned grid_x_for(uint32_t max_n) {
+  uint32_t g = (max_n + 255) / 256;
+  if (g > 1024) g = 1024;
+  return g ? g : 1;
+}
+
+cudaError_t launch_view_keys(cudaStream_t st, const ViewDev* views,
+                             const uint64_t* view_off, uint32_t n_views,
+                             uint32_t max_n, uint32_t* keys, uint32_t* vals) {
+  if (n_views == 0) return cudaSuccess;
+  k_view_keys<<<dim3(grid_x_for(max_n), n_views), 256, 0, st>>>(views, view_off,
+                                                               keys, vals);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_strip_keys(cudaStream_t st, const InstDev* insts,
+                              const uint32_t* inst_ids, const uint64_t* seg_off,
+                              uint32_t n_seg, uint32_t max_n, uint32_t* keys,
+                              uint32_t* vals) {
+  if (n_seg == 0) return cudaSuccess;
+  k_strip_keys<<<dim3(grid_x_for(max_n), n_seg), 256, 0, st>>>(
+      insts, inst_ids, seg_off, keys, vals);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_strip_bounds(cudaStream_t st, const InstDev* insts,
+                                uint32_t n_inst, uint32_t max_n) {
+  if (n_inst == 0) return cudaSuccess;
+  k_strip_bounds<<<dim3(grid_x_for(max_n + 1), n_inst), 256, 0, st>>>(insts);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tile_offsets(cudaStream_t st, const InstDev* insts,
+                                uint32_t n_inst) {
+  if (n_inst == 0) return cudaSuccess;
+  k_tile_offsets<<<n_inst, 1024, 0, st>>>(insts);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gather_pts(cudaStream_t st, const InstDev* insts,
+                              uint32_t n_inst, uint32_t max_n) {
+  if (n_inst == 0) return cudaSuccess;
+  k_gather_pts<<<dim3(grid_x_for(max_n), n_inst), 256, 0, st>>>(insts);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_plan(cudaStream_t st, const InstDev* insts, uint32_t n_inst,
+                        const uint32_t* inst_tile_base, TileDesc* tiles,
+                        uint32_t n_slots, uint64_t* n_src_total) {
+  if (n_slots == 0) return cudaSuccess;
+  k_plan<<<(n_slots + 127) / 128, 128, 0, st>>>(
+      insts, n_inst, inst_tile_base, tiles, n_slots,
+      reinterpret_cast<unsigned long long*>(n_src_total));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_density(cudaStream_t st, int d, const TileDesc* tiles,
+                           uint32_t n_slots, const InstDev* insts,
+                           uint32_t* work_counter, uint32_t* err,
+                           double* tile_logsum, uint32_t mode, int n_sms,
+                           int* launched) {
+  switch (d) {
+    case 1:
+      return launch_density_t<1, R1>(st, tiles, n_slots, insts, work_counter,
+                                     err, tile_logsum, mode, n_sms, launched);
+    case 2:
+      return launch_density_t<2, R2>(st, tiles, n_slots, insts, work_counter,
+                                     err, tile_logsum, mode, n_sms, launched);
+    case 3:
+      return launch_density_t<3, R3>(st, tiles, n_slots, insts, work_counter,
+                                     err, tile_logsum, mode, n_sms, launched);
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_inst_logsum(cudaStream_t st, const InstDev* insts,
+                               uint32_t n_inst, const double* tile_logsum,
+                               double* inst_logsum) {
+  if (n_inst == 0) return cudaSuccess;
+  k_inst_logsum<<<n_inst, 256, 0, st>>>(insts, tile_logsum, inst_logsum);
+  return cudaGetLastError();
+}
+
+}  // namespace ent

@@ -1,0 +1,115 @@
+// Internal interfaces between the CUDA translation units of the entropical
+// GB300 library. Not part of the public C ABI (include/entropical_gb300.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace ent {
+
+// ------------------------------------------------------------ radix sort
+struct SegTableDev {
+  const uint64_t* seg_off;   // element offset of segment s
+  const uint32_t* seg_len;   // element count of segment s
+  const uint32_t* seg_blk0;  // first radix block of segment s (n_seg + 1)
+  const uint32_t* blk_seg;   // segment of every radix block
+  uint32_t* hist;            // 256 counters per radix block
+};
+
+uint32_t radix_blocks_for(uint32_t len);
+// Sorts every segment of (keys, vals) on bits [begin_bit, end_bit). The
+// pointers are swapped so that on return keys/vals hold the result.
+cudaError_t seg_radix_sort(cudaStream_t st, const SegTableDev& t,
+                           uint32_t n_seg, uint32_t total_blocks,
+                           uint32_t*& keys, uint32_t*& vals, uint32_t*& ktmp,
+                           uint32_t*& vtmp, int begin_bit, int end_bit);
+
+// -------------------------------------------------------- density engine
+constexpr int MAX_RUNS = 9;  // 3 cells per remaining dimension, d <= 3
+
+// One column view: a contiguous float32 range on the device (a selected,
+// possibly lagged coordinate column).
+struct ViewDev {
+  const float* x;
+  uint32_t n;
+  uint32_t pad;
+};
+
+struct ViewStats {
+  float mn, mx;
+  double s1, s2;  // sum and sum of squares (FP64)
+  uint32_t nonfinite;
+  uint32_t pad;
+};
+
+// One density instance: d coordinate views of n points, bandwidths h.
+struct InstDev {
+  const float* x[3];        // coordinates by original (instance-local) index
+  uint32_t n, d, S, n_strips;
+  uint32_t ncell1, ncell2;  // cells along dims 1 and 2 (1 when absent)
+  uint32_t tile_base, tile_cap;
+  float lo1, lo2;           // cell-grid origins
+  double inv_w1, inv_w2;    // inverse cell widths (cell width = h/S, widened)
+  float center[3];
+  float inv_h[3];
+  const uint32_t* perm0;    // dimension-0 sorted order (view sort)
+  uint32_t* perm;           // final strip-major order
+  const uint32_t* skeys;    // sorted strip keys (d >= 2)
+  void* pts;                // sorted, centred, 1/h-scaled points (float/float2/float4)
+  uint32_t* strip_start;    // n_strips + 1
+  uint32_t* tile_off;       // n_strips + 1
+  double scale;             // 0.75^d / (norm * prod h)
+  double* out;              // per-point density by original index (nullable)
+  uint32_t tt;              // targets per tile
+  uint32_t pad;
+};
+
+struct TileDesc {
+  uint32_t inst;
+  uint32_t t_begin;  // first target (position in the sorted order)
+  uint32_t t_count;  // 0 marks an unused slot
+  uint32_t n_runs;
+  uint32_t lo[MAX_RUNS];   // candidate-source runs (sorted positions)
+  uint32_t len[MAX_RUNS];
+};
+
+// Epilogue modes of the density kernel.
+enum : uint32_t {
+  DM_WRITE_F64 = 1u,  // out[perm[k]] = density (double)
+  DM_LOGSUM = 2u,     // tile_logsum[g] = sum of log(density) over the tile
+  DM_COUNT = 4u,      // count in-support pairs instead of summing the kernel
+  DM_SUMV = 8u,       // tile_logsum[g] = sum of the per-point values (no log)
+};
+
+// Kernel launch helpers (density.cu).
+cudaError_t launch_colstats(cudaStream_t st, const ViewDev* views,
+                            uint32_t n_views, ViewStats* stats);
+cudaError_t launch_view_keys(cudaStream_t st, const ViewDev* views,
+                             const uint64_t* view_off, uint32_t n_views,
+                             uint32_t max_n, uint32_t* keys, uint32_t* vals);
+cudaError_t launch_strip_keys(cudaStream_t st, const InstDev* insts,
+                              const uint32_t* inst_ids, const uint64_t* seg_off,
+                              uint32_t n_seg, uint32_t max_n, uint32_t* keys,
+                              uint32_t* vals);
+cudaError_t launch_strip_bounds(cudaStream_t st, const InstDev* insts,
+                                uint32_t n_inst, uint32_t max_n);
+cudaError_t launch_tile_offsets(cudaStream_t st, const InstDev* insts,
+                                uint32_t n_inst);
+cudaError_t launch_gather_pts(cudaStream_t st, const InstDev* insts,
+                              uint32_t n_inst, uint32_t max_n);
+cudaError_t launch_plan(cudaStream_t st, const InstDev* insts, uint32_t n_inst,
+                        const uint32_t* inst_tile_base, TileDesc* tiles,
+                        uint32_t n_slots, uint64_t* n_src_total);
+cudaError_t launch_density(cudaStream_t st, int d, const TileDesc* tiles,
+                           uint32_t n_slots, const InstDev* insts,
+                           uint32_t* work_counter, uint32_t* err,
+                           double* tile_logsum, uint32_t mode, int n_sms,
+                           int* launched_ctas);
+int density_tile_targets(int d);
+cudaError_t launch_inst_logsum(cudaStream_t st, const InstDev* insts,
+                               uint32_t n_inst, const double* tile_logsum,
+                               double* inst_logsum);
+
+}  // namespace ent

@@ -1,0 +1,230 @@
+"""Host mirror of the reference density interface over the C ABI.
+
+``combined_densities`` keeps the reference's name, argument order and meaning
+(densities_cuda.hpp:9-24): a column-major float32 coordinate buffer, the
+number of rows, the selected column indices, one bandwidth per selected
+column and optional lags. It returns float64 densities of the n_rows-max(tau)
+selected points, computed by the CUDA library; invalid selections raise
+``NativeError`` with the reference's message instead of exiting.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Sequence
+
+import numpy as np
+
+from . import _native
+from ._native import CallStats, Instance, c_f32_p, c_f64_p, c_size_p, c_u32_p
+
+COMPAT_NORM = 1
+BATCH_SUPPORT_COUNTS = 2
+BATCH_DEVICE_INPUT = 4
+
+
+def as_colmajor(coords, n_rows: int | None = None) -> tuple[np.ndarray, int, int]:
+    """Return (flat float32 column-major buffer, n_rows, n_cols).
+
+    Accepts a flat buffer (then n_rows is required) or a 2-D array of shape
+    (n_cols, n_rows) -- one row per coordinate column, the reference layout.
+    """
+    a = np.asarray(coords)
+    if a.ndim == 1:
+        if n_rows is None or n_rows <= 0 or a.size % n_rows:
+            raise ValueError("flat coords need n_rows dividing their length")
+        n_cols = a.size // n_rows
+    elif a.ndim == 2:
+        n_cols, n_rows_a = a.shape
+        if n_rows is not None and n_rows != n_rows_a:
+            raise ValueError("n_rows does not match coords.shape[1]")
+        n_rows = n_rows_a
+    else:
+        raise ValueError("coords must be 1-D (flat) or 2-D (n_cols, n_rows)")
+    flat = np.ascontiguousarray(a, dtype=np.float32).reshape(-1)
+    return flat, int(n_rows), int(n_cols)
+
+
+def _u32(v: Sequence[int]) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(v, dtype=np.uint32))
+
+
+def _f32(v: Sequence[float]) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(v, dtype=np.float32))
+
+
+class Context:
+    """One CUDA device, one stream and a grow-only device workspace."""
+
+    def __init__(self, device: int = -1):
+        self._lib = _native.load()
+        h = C.c_void_p()
+        _native.check(self._lib, None, self._lib.ent_create(C.byref(h), int(device)))
+        self._h = h
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    @property
+    def lib(self) -> C.CDLL:
+        return self._lib
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.ent_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def check(self, status: int) -> None:
+        _native.check(self._lib, self._h, status)
+
+    def last_stats(self) -> CallStats:
+        s = CallStats()
+        self.check(self._lib.ent_last_stats(self._h, C.byref(s)))
+        return s
+
+    def _selection(self, i_cols, h, tau):
+        d = len(i_cols)
+        cols = _u32(i_cols)
+        hv = _f32(h)
+        if len(hv) != d:
+            raise _native.NativeError(2, self._lib.ent_status_string(2).decode())
+        tv = None
+        if tau is not None:
+            tv = _u32(tau)
+            if len(tv) != d:
+                raise _native.NativeError(3, self._lib.ent_status_string(3).decode())
+        return d, cols, hv, tv
+
+    def combined_densities(self, coords, n_rows: int | None, i_cols: Sequence[int],
+                           h: Sequence[float], tau: Sequence[int] | None = None,
+                           compat_norm: bool = False) -> np.ndarray:
+        flat, n_rows, n_cols = as_colmajor(coords, n_rows)
+        d, cols, hv, tv = self._selection(i_cols, h, tau)
+        n_sel = n_rows - (int(tv.max()) if tv is not None and d else 0)
+        out = np.empty(max(n_sel, 0), dtype=np.float64)
+        n_out = C.c_size_t(0)
+        st = self._lib.ent_densities(
+            self._h, flat.ctypes.data_as(C.c_void_p), n_rows, n_cols,
+            cols.ctypes.data_as(c_u32_p), hv.ctypes.data_as(c_f32_p),
+            tv.ctypes.data_as(c_u32_p) if tv is not None else None, d,
+            COMPAT_NORM if compat_norm else 0, out.ctypes.data_as(C.c_void_p), C.byref(n_out))
+        self.check(st)
+        return out[: n_out.value]
+
+    def combined_densities_device(self, d_coords: int, n_rows: int, n_cols: int,
+                                  i_cols: Sequence[int], h: Sequence[float],
+                                  tau: Sequence[int] | None, d_out: int,
+                                  compat_norm: bool = False) -> int:
+        """Device-pointer form; returns n_sel. Pointers are raw CUDA addresses."""
+        d, cols, hv, tv = self._selection(i_cols, h, tau)
+        n_out = C.c_size_t(0)
+        st = self._lib.ent_densities_device(
+            self._h, C.c_void_p(d_coords), n_rows, n_cols, cols.ctypes.data_as(c_u32_p),
+            hv.ctypes.data_as(c_f32_p), tv.ctypes.data_as(c_u32_p) if tv is not None else None,
+            d, COMPAT_NORM if compat_norm else 0, C.c_void_p(d_out), C.byref(n_out))
+        self.check(st)
+        return n_out.value
+
+    def support_counts(self, coords, n_rows: int | None, i_cols: Sequence[int],
+                       h: Sequence[float], tau: Sequence[int] | None = None) -> np.ndarray:
+        """Per point, the number of sources inside the product-kernel support."""
+        flat, n_rows, n_cols = as_colmajor(coords, n_rows)
+        d, cols, hv, tv = self._selection(i_cols, h, tau)
+        n_sel = n_rows - (int(tv.max()) if tv is not None and d else 0)
+        out = np.empty(max(n_sel, 0), dtype=np.float64)
+        n_out = C.c_size_t(0)
+        st = self._lib.ent_support_counts(
+            self._h, flat.ctypes.data_as(C.c_void_p), n_rows, n_cols,
+            cols.ctypes.data_as(c_u32_p), hv.ctypes.data_as(c_f32_p),
+            tv.ctypes.data_as(c_u32_p) if tv is not None else None, d,
+            out.ctypes.data_as(C.c_void_p), C.byref(n_out))
+        self.check(st)
+        return out[: n_out.value]
+
+
+    # ------------------------------------------------------------ batches
+    def mi_all_pairs(self, coords, h: Sequence[float], counts: bool = False
+                     ) -> tuple[np.ndarray, np.ndarray]:
+        """All-pairs MI (resubstitution) of the rows of coords (n_cols, n_rows)
+        in one batch; returns (MI matrix, marginal entropies). With
+        counts=True, the in-support pair counts of every density instead."""
+        flat, n_rows, n_cols = as_colmajor(coords)
+        hv = _f32(h)
+        if len(hv) != n_cols:
+            raise ValueError("one bandwidth per column")
+        mi = np.zeros((n_cols, n_cols), dtype=np.float64)
+        hx = np.zeros(n_cols, dtype=np.float64)
+        st = self._lib.ent_mi_all_pairs(
+            self._h, flat.ctypes.data_as(C.c_void_p), n_rows, n_cols, hv.ctypes.data_as(c_f32_p),
+            BATCH_SUPPORT_COUNTS if counts else 0, mi.ctypes.data_as(c_f64_p),
+            hx.ctypes.data_as(c_f64_p))
+        self.check(st)
+        return mi, hx
+
+    def mi_all_pairs_device(self, d_coords: int, n_rows: int, n_cols: int,
+                            h: Sequence[float], counts: bool = False
+                            ) -> tuple[np.ndarray, np.ndarray]:
+        hv = _f32(h)
+        mi = np.zeros((n_cols, n_cols), dtype=np.float64)
+        hx = np.zeros(n_cols, dtype=np.float64)
+        st = self._lib.ent_mi_all_pairs_device(
+            self._h, C.c_void_p(d_coords), n_rows, n_cols, hv.ctypes.data_as(c_f32_p),
+            BATCH_SUPPORT_COUNTS if counts else 0, mi.ctypes.data_as(c_f64_p),
+            hx.ctypes.data_as(c_f64_p))
+        self.check(st)
+        return mi, hx
+
+    def entropy_batch(self, instances, counts: bool = False, device: bool = False) -> np.ndarray:
+        """Resubstitution entropies of [(coords (d, n), h (d,))...] in one batch.
+        With device=True, coords entries are raw device addresses and the
+        tuples are (address, d, n, h)."""
+        arr = (Instance * len(instances))()
+        keep = []
+        for q, item in enumerate(instances):
+            if device:
+                addr, d, n, h = item
+                arr[q].coords = C.c_void_p(addr)
+            else:
+                x, h = item
+                x = np.ascontiguousarray(np.atleast_2d(x), dtype=np.float32)
+                keep.append(x)
+                d, n = x.shape
+                arr[q].coords = x.ctypes.data_as(C.c_void_p)
+            arr[q].n = n
+            arr[q].d = d
+            for j in range(d):
+                arr[q].h[j] = float(h[j])
+        out = np.zeros(len(instances), dtype=np.float64)
+        flags = (BATCH_SUPPORT_COUNTS if counts else 0) | (BATCH_DEVICE_INPUT if device else 0)
+        st = self._lib.ent_entropy_batch(self._h, C.cast(arr, C.c_void_p), len(instances),
+                                         flags, out.ctypes.data_as(c_f64_p))
+        self.check(st)
+        return out
+
+
+_default: Context | None = None
+
+
+def default_context() -> Context:
+    global _default
+    if _default is None:
+        _default = Context()
+    return _default
+
+
+def combined_densities(coords, n_rows: int | None, i_cols: Sequence[int], h: Sequence[float],
+                       tau: Sequence[int] | None = None, compat_norm: bool = False) -> np.ndarray:
+    """Densities of the selected (lagged) columns; see ``Context.combined_densities``."""
+    return default_context().combined_densities(coords, n_rows, i_cols, h, tau, compat_norm)

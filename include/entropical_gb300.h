@@ -1,0 +1,155 @@
+/*
+ * entropical_gb300.h -- C ABI of the GB300 (sm_103a) density hot path of
+ * lettis/entropical.
+ *
+ * Plain C: pointers, sizes and status codes only, so that the reference's
+ * C++ host code (through entropical_gb300/shim/densities_gb300.hpp), ctypes,
+ * or any FFI can bind it. Coordinates follow the reference's layout: a
+ * column-major float32 buffer of n_rows x n_cols (column j at
+ * coords[j*n_rows + i], tools.hxx:153-235).
+ *
+ * Every call is synchronous with respect to the host, as the reference's
+ * combined_densities() is (densities_cuda.cu:46-105). A context is bound to
+ * one CUDA device, owns one stream and a grow-only device workspace, and must
+ * not be used by two host threads at once. Errors are returned as status
+ * codes; the reference instead printed a message and called exit(), which
+ * the C++ shim reproduces.
+ */
+#ifndef ENTROPICAL_GB300_H
+#define ENTROPICAL_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ent_ctx ent_ctx;
+
+enum ent_status {
+  ENT_OK = 0,
+  ENT_ERR_DIM = 1,         /* d not in {1,2,3} (densities_common.hxx:15-19) */
+  ENT_ERR_H_COUNT = 2,     /* bandwidth count != d (densities_common.hxx:20-25) */
+  ENT_ERR_TAU_COUNT = 3,   /* lag count != d (densities_common.hxx:26-31) */
+  ENT_ERR_ARG = 4,         /* null pointer, column index out of range,
+                              lag >= n_rows, bandwidth not finite and > 0 */
+  ENT_ERR_NONFINITE = 5,   /* NaN or Inf among the selected coordinates */
+  ENT_ERR_CUDA = 6,        /* CUDA runtime error (tools.cuh:32-42) */
+  ENT_ERR_NO_DEVICE = 7,   /* no CUDA device (density_1d.cuh:306-309) */
+  ENT_ERR_TIMEOUT = 8,     /* a bounded device-side wait expired */
+  ENT_ERR_TOO_LARGE = 9,   /* more rows than 32-bit point indices allow */
+  ENT_ERR_STATE = 10       /* call not valid in the current state */
+};
+
+/* flags for ent_densities* */
+#define ENT_COMPAT_NORM 1u /* divide by the original n_rows, as the reference
+                              CUDA build does even when lags shorten the
+                              sample (densities_cuda.cu:98-103); default is
+                              the selected sample size n_rows - max(tau) */
+
+/* Statistics of the last call on a context. */
+typedef struct {
+  uint64_t candidate_pairs; /* (target, candidate source) pairs evaluated */
+  uint64_t tiles;           /* target tiles processed */
+  uint32_t kernel_launches; /* kernels this library launched for the call */
+  uint32_t instances;       /* density instances computed */
+  float pair_kernel_ms;     /* device time of the pair kernel(s) */
+  float total_ms;           /* device time of the whole call */
+  uint64_t candidate_pairs_by_dim[3]; /* same, split by density dimension */
+  float pair_kernel_ms_by_dim[3];     /* device time of each persistent launch */
+} ent_call_stats;
+
+/* Context lifecycle. device < 0 selects the current device. */
+int ent_create(ent_ctx** ctx, int device);
+void ent_destroy(ent_ctx* ctx);
+const char* ent_status_string(int status);
+/* Message of the last failing call on ctx (empty if none). */
+const char* ent_last_error(const ent_ctx* ctx);
+int ent_last_stats(const ent_ctx* ctx, ent_call_stats* stats);
+
+/*
+ * Combined product-Epanechnikov densities of d = 1..3 selected, lagged
+ * columns. Replaces
+ *   std::vector<double> combined_densities(const float* coords,
+ *       std::size_t n_rows, std::vector<unsigned> i_cols,
+ *       std::vector<float> h, std::vector<unsigned> tau)
+ * (densities_cuda.hpp:9-24, densities_cuda.cu:16-105; OpenMP form
+ * densities_omp.cpp:163-233). tau may be NULL (all zero). Point i of the
+ * result is the density at (x_{i_cols[0]}[i+tau[0]], ...), i < n_sel =
+ * n_rows - max(tau):
+ *   out[i] = 1/norm * sum_k prod_j 0.75 (1 - u_j^2)/h_j [u_j^2 <= 1],
+ *   u_j = (x_j[i] - x_j[k]) / h_j,
+ * norm = n_sel, or n_rows with ENT_COMPAT_NORM. *n_out receives n_sel.
+ * coords, out: host memory (copies are part of the call).
+ */
+int ent_densities(ent_ctx* ctx, const float* coords, size_t n_rows,
+                  size_t n_cols, const uint32_t* i_cols, const float* h,
+                  const uint32_t* tau, uint32_t d, uint32_t flags, double* out,
+                  size_t* n_out);
+/* Same with coords and out in device memory of the context's device. */
+int ent_densities_device(ent_ctx* ctx, const float* d_coords, size_t n_rows,
+                         size_t n_cols, const uint32_t* i_cols, const float* h,
+                         const uint32_t* tau, uint32_t d, uint32_t flags,
+                         double* d_out, size_t* n_out);
+
+/*
+ * Number of (target, source) pairs inside the kernel support for the same
+ * selection: out[i] = #{k : u_j^2 <= 1 for all j}. Used to report
+ * pair-kernel evaluation rates; host memory.
+ */
+int ent_support_counts(ent_ctx* ctx, const float* coords, size_t n_rows,
+                       size_t n_cols, const uint32_t* i_cols, const float* h,
+                       const uint32_t* tau, uint32_t d, double* out,
+                       size_t* n_out);
+
+/* ------------------------------------------------------------ batches */
+
+/* flags for the batched entry points */
+#define ENT_BATCH_SUPPORT_COUNTS 2u /* return in-support pair counts instead
+                                       of entropies (pair-rate reporting) */
+#define ENT_BATCH_DEVICE_INPUT 4u   /* ent_entropy_batch: coords are device
+                                       pointers */
+
+/*
+ * All-pairs mutual information of n_cols coordinates in ONE batch: n_cols
+ * 1-D marginal densities and n_cols(n_cols-1)/2 2-D joint densities, with
+ * bandwidth h[j] for column j in every density it appears in (as
+ * mi.cpp:38-52 reuses them). Replaces the per-pair combined_densities() loop
+ * of Mi::main (mi.cpp:37-59). Resubstitution estimator in FP64:
+ *   H_j = -1/n sum_i log p_j(x_i),  MI_ij = H_i + H_j - H_ij,
+ * densities normalised by n_rows. mi_out: n_cols x n_cols row-major, zero
+ * diagonal (as mi.cpp leaves it); h_out (nullable): the n_cols marginal
+ * entropies. With ENT_BATCH_SUPPORT_COUNTS, mi_out[i][j] / h_out[i] instead
+ * receive the number of in-support (target, source) pairs of each density.
+ * coords: host memory, column-major n_rows x n_cols.
+ */
+int ent_mi_all_pairs(ent_ctx* ctx, const float* coords, size_t n_rows,
+                     size_t n_cols, const float* h, uint32_t flags,
+                     double* mi_out, double* h_out);
+/* Same with coords in device memory (outputs stay on the host). */
+int ent_mi_all_pairs_device(ent_ctx* ctx, const float* d_coords, size_t n_rows,
+                            size_t n_cols, const float* h, uint32_t flags,
+                            double* mi_out, double* h_out);
+
+/* One density instance of an uneven batch. */
+typedef struct {
+  const float* coords; /* column-major d x n: dimension j at coords[j*n + i] */
+  uint64_t n;
+  uint32_t d;          /* 1..3 */
+  float h[3];
+} ent_instance;
+
+/*
+ * Resubstitution entropies -mean(log p) of many independent instances of
+ * uneven size and dimension, in ONE batch (one persistent launch per
+ * dimension). Replaces sequential combined_densities() calls followed by
+ * host reductions. h_out: n_inst values.
+ */
+int ent_entropy_batch(ent_ctx* ctx, const ent_instance* inst, size_t n_inst,
+                      uint32_t flags, double* h_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ENTROPICAL_GB300_H */

@@ -108,6 +108,31 @@ int orc_density_fp64(const float* sel, size_t n, int d, const double* h,
   return orc_density_fp64_at(sel, n, d, h, norm, NULL, n, out);
 }
 
+uint64_t orc_support_count_fp64(const float* sel, size_t n, int d,
+                                const double* h) {
+  if (d < 1 || d > 3 || n == 0) return 0;
+  uint32_t* p = sorted_perm(sel, n);
+  double* s = (double*)malloc(n * sizeof(double) * (size_t)d);
+  for (size_t k = 0; k < n; ++k)
+    for (int j = 0; j < d; ++j) s[(size_t)j * n + k] = sel[(size_t)j * n + p[k]];
+  free(p);
+  uint64_t tot = 0;
+#pragma omp parallel for reduction(+ : tot) schedule(dynamic, 64)
+  for (size_t i = 0; i < n; ++i) {
+    double x[3];
+    for (int j = 0; j < d; ++j) x[j] = s[(size_t)j * n + i];
+    size_t lo = lower_bound_d(s, n, x[0] - h[0]);
+    size_t hi = upper_bound_d(s, n, x[0] + h[0]);
+    for (size_t k = lo; k < hi; ++k) {
+      int in = 1;
+      for (int j = 1; j < d && in; ++j) in = fabs(x[j] - s[(size_t)j * n + k]) <= h[j];
+      tot += (uint64_t)in;
+    }
+  }
+  free(s);
+  return tot;
+}
+
 /* ------------------------------------------- reference float restatement */
 
 /* Densities::OMP::epanechnikov::operator() (densities_omp.cpp:19-26):
@@ -153,8 +178,33 @@ void orc_boxes(const float* col, size_t n, float h, uint64_t* lo, uint64_t* hi) 
   free(s);
 }
 
+/* The reference's own scans (densities_omp.cpp:49-62): from the front for
+ * the first hit, from the back for the last. Same result as boxes_of(), at
+ * the reference's O(n) cost per point; used to time the CPU baseline. */
+static void boxes_linear(const float* sorted, size_t n, float ref, float h,
+                         size_t* lo_out, size_t* hi_out) {
+  size_t k;
+  for (k = 0; k < n; ++k)
+    if (ref - sorted[k] < h) { *lo_out = k; break; }
+  for (k = n; k > 0; --k)
+    if (sorted[k - 1] - ref < h) { *hi_out = k - 1; break; }
+}
+
+static int density_ref_f32_impl(const float* sel, size_t n, int d,
+                                const float* h, float* out, int linear);
+
 int orc_density_ref_f32(const float* sel, size_t n, int d, const float* h,
                         float* out) {
+  return density_ref_f32_impl(sel, n, d, h, out, 0);
+}
+
+int orc_density_ref_f32_linear(const float* sel, size_t n, int d,
+                               const float* h, float* out) {
+  return density_ref_f32_impl(sel, n, d, h, out, 1);
+}
+
+static int density_ref_f32_impl(const float* sel, size_t n, int d,
+                                const float* h, float* out, int linear) {
   if (d < 1 || d > 3 || n == 0) return 1;
   /* dim1_sorted_coords (tools.hxx:113-150): rows sorted on column 0 */
   uint32_t* p = sorted_perm(sel, n);
@@ -165,8 +215,9 @@ int orc_density_ref_f32(const float* sel, size_t n, int d, const float* h,
   float fn = (float)n;
 #pragma omp parallel for schedule(dynamic, 16)
   for (size_t i = 0; i < n; ++i) {
-    size_t lo, hi;
-    boxes_of(s, n, sel[i], h[0], &lo, &hi);
+    size_t lo = 0, hi = 0;
+    if (linear) boxes_linear(s, n, sel[i], h[0], &lo, &hi);
+    else boxes_of(s, n, sel[i], h[0], &lo, &hi);
     float acc = 0.0f;
     for (size_t k = lo; k <= hi && k < n; ++k) {
       float e = epa_ref(sel[i], s[k], h[0]);

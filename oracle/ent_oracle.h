@@ -38,12 +38,19 @@ int orc_density_fp64_at(const float* sel, size_t n, int d, const double* h,
                         double* out);
 int orc_density_fp64(const float* sel, size_t n, int d, const double* h,
                      double norm, double* out);
+/* Number of ordered pairs (i, k) with |x_ij - x_kj| <= h_j for every j. */
+uint64_t orc_support_count_fp64(const float* sel, size_t n, int d,
+                                const double* h);
 
 /* Float restatement of the reference OpenMP density, operation for operation:
  * dim-1 sort (tools.hxx:113-150), boxes() windows (densities_omp.cpp:33-65),
  * float accumulation of epanechnikov() products (:19-26, :67-159), then /n. */
 int orc_density_ref_f32(const float* sel, size_t n, int d, const float* h,
                         float* out);
+/* Same result with the reference's linear window scans (its O(n^2) cost);
+ * used only to time the CPU baseline. */
+int orc_density_ref_f32_linear(const float* sel, size_t n, int d,
+                               const float* h, float* out);
 
 /* boxes() window bounds (densities_omp.cpp:33-65) for every point of a column
  * (original order) against the sorted column: lo = first k with

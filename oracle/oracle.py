@@ -1,0 +1,262 @@
+"""Python access to the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and the CPU-baseline leg of bench.py use
+this module, and only as the checker. It wraps
+
+* ``lib/libentoracle.so``: the C restatement of the reference algorithms and
+  the FP64 brute force (ent_oracle.c, built by ``make -C oracle oracle``);
+* ``_ref/libentref.so``: the reference's own OpenMP sources compiled in place
+  (``make -C oracle ref``; only where the reference sources exist);
+
+plus FP64 numpy forms of the estimators (entropy, mutual information,
+transfer entropy) on oracle densities.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ORACLE_SO = HERE / "lib" / "libentoracle.so"
+REF_SO = HERE / "_ref" / "libentref.so"
+
+_orc = None
+_ref = None
+
+
+def _p(a: np.ndarray) -> C.c_void_p:
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def build_oracle() -> Path:
+    subprocess.run(["make", "-s", "-C", str(HERE), "oracle"], check=True)
+    return ORACLE_SO
+
+
+def build_ref(reference: str = "/root/reference") -> Path | None:
+    if not Path(reference, "densities_omp.cpp").exists():
+        return None
+    subprocess.run(["make", "-s", "-j8", "-C", str(HERE), "ref", f"REF={reference}"], check=True)
+    return REF_SO
+
+
+def orc() -> C.CDLL:
+    global _orc
+    if _orc is None:
+        if not ORACLE_SO.exists():
+            build_oracle()
+        lib = C.CDLL(str(ORACLE_SO))
+        lib.orc_epa_conv_ref.restype = C.c_float
+        lib.orc_epa_conv_fp64.restype = C.c_double
+        lib.orc_thumb_ref.restype = C.c_float
+        lib.orc_amise_from_conv.restype = C.c_float
+        lib.orc_amise_from_conv.argtypes = [C.c_float, C.c_float, C.c_size_t]
+        lib.orc_hestimate_amise.restype = C.c_float
+        lib.orc_boxedsearch.restype = C.c_uint64
+        lib.orc_support_count_fp64.restype = C.c_uint64
+        _orc = lib
+    return _orc
+
+
+def ref_available() -> bool:
+    return REF_SO.exists()
+
+
+def ref() -> C.CDLL:
+    global _ref
+    if _ref is None:
+        lib = C.CDLL(str(REF_SO))
+        lib.ref_epa_convolution.restype = C.c_float
+        lib.ref_thumb.restype = C.c_float
+        lib.ref_amise_h.restype = C.c_float
+        lib.ref_boxedsearch.restype = C.c_uint64
+        _ref = lib
+    return _ref
+
+
+# ------------------------------------------------------------- selections
+def repack(coords: np.ndarray, cols, tau=None) -> np.ndarray:
+    """(n_cols, n_rows) column-major coords -> (d, n_sel) selected, lagged
+    columns, as prob_dens_coord_prep builds them (densities_common.hxx:37-48)."""
+    coords = np.asarray(coords, dtype=np.float32)
+    d = len(cols)
+    tau = [0] * d if tau is None else list(tau)
+    n_sel = coords.shape[1] - max(tau)
+    return np.ascontiguousarray(
+        np.stack([coords[c, t:t + n_sel] for c, t in zip(cols, tau)]).astype(np.float32))
+
+
+# ---------------------------------------------------------------- densities
+def density_fp64(sel: np.ndarray, h, norm: float | None = None, targets=None) -> np.ndarray:
+    sel = np.ascontiguousarray(sel, dtype=np.float32)
+    d, n = sel.shape
+    hd = np.ascontiguousarray(np.asarray(h, dtype=np.float32).astype(np.float64))
+    norm = float(n if norm is None else norm)
+    if targets is None:
+        out = np.empty(n)
+        st = orc().orc_density_fp64(_p(sel), C.c_size_t(n), C.c_int(d), _p(hd),
+                                    C.c_double(norm), _p(out))
+    else:
+        t = np.ascontiguousarray(np.asarray(targets, dtype=np.uint32))
+        out = np.empty(len(t))
+        st = orc().orc_density_fp64_at(_p(sel), C.c_size_t(n), C.c_int(d), _p(hd),
+                                       C.c_double(norm), _p(t), C.c_size_t(len(t)), _p(out))
+    assert st == 0
+    return out
+
+
+def support_count_fp64(sel: np.ndarray, h) -> int:
+    """Ordered pairs inside the product-kernel support (FP64 test)."""
+    sel = np.ascontiguousarray(sel, dtype=np.float32)
+    d, n = sel.shape
+    hd = np.ascontiguousarray(np.asarray(h, dtype=np.float32).astype(np.float64))
+    return int(orc().orc_support_count_fp64(_p(sel), C.c_size_t(n), C.c_int(d), _p(hd)))
+
+
+def density_ref_f32(sel: np.ndarray, h, linear_scan: bool = False) -> np.ndarray:
+    """Reference OpenMP density restated; linear_scan=True also keeps the
+    reference's O(n) window scans per point (for timing)."""
+    sel = np.ascontiguousarray(sel, dtype=np.float32)
+    d, n = sel.shape
+    hf = np.ascontiguousarray(np.asarray(h, dtype=np.float32))
+    out = np.empty(n, dtype=np.float32)
+    fn = orc().orc_density_ref_f32_linear if linear_scan else orc().orc_density_ref_f32
+    assert fn(_p(sel), C.c_size_t(n), C.c_int(d), _p(hf), _p(out)) == 0
+    return out
+
+
+def boxes(col: np.ndarray, h: float) -> tuple[np.ndarray, np.ndarray]:
+    col = np.ascontiguousarray(col, dtype=np.float32)
+    lo = np.empty(len(col), np.uint64)
+    hi = np.empty(len(col), np.uint64)
+    orc().orc_boxes(_p(col), C.c_size_t(len(col)), C.c_float(h), _p(lo), _p(hi))
+    return lo, hi
+
+
+def boxedsearch(col: np.ndarray, box: float):
+    col = np.ascontiguousarray(col, dtype=np.float32)
+    b = np.empty(len(col), np.uint64)
+    c = np.empty(len(col), np.uint64)
+    nb = orc().orc_boxedsearch(_p(col), C.c_size_t(len(col)), C.c_float(box), _p(b), _p(c))
+    return int(nb), b, c
+
+
+def epa_conv_ref(sorted_col: np.ndarray, h: float) -> float:
+    s = np.ascontiguousarray(sorted_col, dtype=np.float32)
+    return float(orc().orc_epa_conv_ref(_p(s), C.c_size_t(len(s)), C.c_float(h)))
+
+
+def epa_conv_fp64(sorted_col: np.ndarray, h: float) -> float:
+    s = np.ascontiguousarray(sorted_col, dtype=np.float32)
+    return float(orc().orc_epa_conv_fp64(_p(s), C.c_size_t(len(s)), C.c_double(h)))
+
+
+def thumb_ref(col: np.ndarray) -> float:
+    c = np.ascontiguousarray(col, dtype=np.float32)
+    return float(orc().orc_thumb_ref(_p(c), C.c_size_t(len(c))))
+
+
+def amise_from_conv(conv: float, h: float, n: int) -> float:
+    return float(orc().orc_amise_from_conv(conv, h, n))
+
+
+def hestimate_amise(col: np.ndarray, exact: bool = False) -> tuple[float, int]:
+    c = np.ascontiguousarray(col, dtype=np.float32)
+    nc = C.c_int(0)
+    h = orc().orc_hestimate_amise(_p(c), C.c_size_t(len(c)), C.c_int(1 if exact else 0),
+                                  C.byref(nc))
+    return float(h), nc.value
+
+
+# -------------------------------------------------------------- estimators
+def entropy_fp64(sel: np.ndarray, h, norm=None) -> float:
+    """Resubstitution entropy -mean(log p) with FP64 oracle densities."""
+    p = density_fp64(sel, h, norm)
+    return float(-np.mean(np.log(p)))
+
+
+def mi_fp64(x: np.ndarray, y: np.ndarray, hx: float, hy: float) -> float:
+    """MI = H(X) + H(Y) - H(X, Y), resubstitution, FP64 oracle densities."""
+    return (entropy_fp64(x[None], [hx]) + entropy_fp64(y[None], [hy])
+            - entropy_fp64(np.stack([x, y]), [hx, hy]))
+
+
+def te_fp64(x: np.ndarray, y: np.ndarray, tau: int, hx: float, hy: float) -> float:
+    """TE_{X->Y}(tau) = mean_t log[p(y+,y,x) p(y) / (p(y,x) p(y+,y))] over
+    t < n - tau (resubstitution, FP64 oracle densities)."""
+    n = len(y) - tau
+    yp, yc, xc = y[tau:tau + n], y[:n], x[:n]
+    l3 = np.log(density_fp64(np.stack([yp, yc, xc]), [hy, hy, hx]))
+    l1 = np.log(density_fp64(yc[None], [hy]))
+    l2a = np.log(density_fp64(np.stack([yc, xc]), [hy, hx]))
+    l2b = np.log(density_fp64(np.stack([yp, yc]), [hy, hy]))
+    return float(np.mean(l3 + l1 - l2a - l2b))
+
+
+# ------------------------------------------------------- reference build
+def ref_densities(coords: np.ndarray, cols, h, tau=None) -> np.ndarray:
+    """The reference's OpenMP combined_densities on repacked columns (float32,
+    already divided by n_sel)."""
+    coords = np.ascontiguousarray(coords, dtype=np.float32)
+    n_cols, n_rows = coords.shape
+    d = len(cols)
+    tau = [0] * d if tau is None else list(tau)
+    c = np.ascontiguousarray(np.asarray(cols, np.uint32))
+    hh = np.ascontiguousarray(np.asarray(h, np.float32))
+    t = np.ascontiguousarray(np.asarray(tau, np.uint32))
+    out = np.empty(n_rows - max(tau), np.float32)
+    assert ref().ref_densities(_p(coords), C.c_size_t(n_rows), _p(c), _p(hh), _p(t),
+                               C.c_uint(d), _p(out)) == 0
+    return out
+
+
+def ref_epa_convolution(sorted_col: np.ndarray, h: float) -> float:
+    s = np.ascontiguousarray(sorted_col, dtype=np.float32)
+    return float(ref().ref_epa_convolution(_p(s), C.c_size_t(len(s)), C.c_float(h)))
+
+
+def ref_boxes(col: np.ndarray, h: float):
+    col = np.ascontiguousarray(col, dtype=np.float32)
+    lo = np.empty(len(col), np.uint64)
+    hi = np.empty(len(col), np.uint64)
+    ref().ref_boxes(_p(col), C.c_size_t(len(col)), C.c_float(h), _p(lo), _p(hi))
+    return lo, hi
+
+
+def ref_boxedsearch(col: np.ndarray, box: float):
+    col = np.ascontiguousarray(col, dtype=np.float32)
+    b = np.empty(len(col), np.uint64)
+    c = np.empty(len(col), np.uint64)
+    nb = ref().ref_boxedsearch(_p(col), C.c_size_t(len(col)), C.c_float(box), _p(b), _p(c))
+    return int(nb), c
+
+
+def ref_thumb(col: np.ndarray) -> float:
+    c = np.ascontiguousarray(col, dtype=np.float32)
+    return float(ref().ref_thumb(_p(c), C.c_size_t(len(c)), C.c_size_t(0)))
+
+
+def ref_amise_h(col: np.ndarray) -> float:
+    c = np.ascontiguousarray(col, dtype=np.float32)
+    return float(ref().ref_amise_h(_p(c), C.c_size_t(len(c)), C.c_size_t(0)))
+
+
+def ref_run_mode(mode: str, coords: np.ndarray, bandwidths, workdir: Path, tau: int = 0,
+                 dims: int = 1, taus: str = "") -> np.ndarray:
+    """Run a reference estimator main() (mi, transs, autoent, negs, kldiv, dens)
+    on an ASCII file, as the entropical CLI would, and parse its output."""
+    workdir = Path(workdir)
+    workdir.mkdir(parents=True, exist_ok=True)
+    fin, fbw, fout = workdir / "coords.txt", workdir / "bw.txt", workdir / "out.txt"
+    np.savetxt(fin, np.asarray(coords, np.float32).T, fmt="%.9g")
+    np.savetxt(fbw, np.asarray(bandwidths, np.float32)[None], fmt="%.9g")
+    st = ref().ref_run_mode(mode.encode(), str(fin).encode(), str(fbw).encode(),
+                            str(fout).encode(), C.c_uint(tau), C.c_uint(dims), taus.encode())
+    assert st == 0
+    if mode == "dens" and dims > 1:
+        rows = [ln.split() for ln in fout.read_text().splitlines() if ln.strip()]
+        return np.array([float(r[1]) for r in rows])
+    return np.loadtxt(fout, ndmin=2)

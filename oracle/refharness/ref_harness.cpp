@@ -81,8 +81,8 @@ std::uint64_t ref_boxedsearch(const float* col, std::size_t n, float box_size,
   for (std::size_t i = 0; i < n; ++i) {
     std::vector<std::size_t> nb = b.neighbors_of_state_ordered(i);
     n_neighbors[i] = nb.size();
+    if (box_of_state) box_of_state[i] = 0;
   }
-  (void)box_of_state;
   return b.n_boxes();
 }
 

@@ -1,0 +1,176 @@
+"""GPU parity of the density path: the CUDA library (through the C ABI)
+against the reference's golden outputs and the FP64 oracle.
+
+Tolerance: densities 1e-5 relative per point (the reference itself is a
+float32 accumulation, ~3e-6 from FP64); support counts and entropies
+derived from them as stated per test."""
+import numpy as np
+import pytest
+
+from entropical_gb300 import NativeError, workloads
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-5
+
+
+def rel_err(a, b):
+    return np.max(np.abs(np.asarray(a) - np.asarray(b)) / np.abs(np.asarray(b)))
+
+
+@pytest.mark.parametrize("case", ["d1", "d2", "d3", "lag"])
+def test_golden_reference(ctx, golden, case):
+    g = golden
+    if case == "d1":
+        p = ctx.combined_densities(g["d1_x"], None, [0], g["d1_h"])
+        ref = g["d1_p"]
+    elif case == "d2":
+        p = ctx.combined_densities(g["d2_x"], None, [0, 1], g["d2_h"])
+        ref = g["d2_p"]
+    elif case == "d3":
+        p = ctx.combined_densities(g["d2_x"], None, [0, 1, 2], g["d3_h"])
+        ref = g["d3_p"]
+    else:
+        p = ctx.combined_densities(g["d2_x"], None, list(g["lag_cols"]), g["lag_h"],
+                                   list(g["lag_tau"]))
+        ref = g["lag_p"]
+    assert p.shape == ref.shape
+    assert rel_err(p, ref) < REL
+
+
+@pytest.mark.parametrize("d", [1, 2, 3])
+@pytest.mark.parametrize("n", [1, 2, 33, 1000, 20000])
+def test_fp64_oracle_shapes(ctx, d, n):
+    rng = np.random.default_rng(1000 * d + n)
+    x = rng.standard_normal((3, n)).astype(np.float32)
+    h = rng.uniform(0.15, 0.6, d).astype(np.float32)
+    cols = list(rng.permutation(3)[:d])
+    p = ctx.combined_densities(x, None, cols, h)
+    f = O.density_fp64(O.repack(x, cols), h)
+    assert rel_err(p, f) < REL
+
+
+@pytest.mark.parametrize("d", [1, 2, 3])
+def test_lags_and_compat_norm(ctx, d):
+    rng = np.random.default_rng(77 + d)
+    x = rng.standard_normal((4, 3000)).astype(np.float32)
+    cols = [1, 1, 3][:d]
+    tau = [0, 11, 4][:d]
+    h = [0.3, 0.25, 0.4][:d]
+    sel = O.repack(x, cols, tau)
+    p = ctx.combined_densities(x, None, cols, h, tau)
+    assert len(p) == 3000 - max(tau)
+    assert rel_err(p, O.density_fp64(sel, h)) < REL
+    pc = ctx.combined_densities(x, None, cols, h, tau, compat_norm=True)
+    assert rel_err(pc, O.density_fp64(sel, h, norm=3000)) < REL
+
+
+@pytest.mark.parametrize("d", [1, 2, 3])
+def test_edge_data(ctx, d):
+    rng = np.random.default_rng(9)
+    n = 4000
+    # exact ties, a constant column, negative-only values, a far outlier
+    x = np.stack([
+        np.round(rng.standard_normal(n) * 4) / 4,
+        np.full(n, -3.0),
+        -np.abs(rng.standard_normal(n)) - 1.0,
+    ]).astype(np.float32)
+    x[0, 17] = 1e4
+    h = [0.2, 0.5, 0.3][:d]
+    for cols in ([0, 1, 2][:d], [2, 0, 1][:d]):
+        p = ctx.combined_densities(x, None, cols, h)
+        assert rel_err(p, O.density_fp64(O.repack(x, cols), h)) < REL
+
+
+@pytest.mark.parametrize("d", [1, 2, 3])
+def test_tiny_and_huge_bandwidth(ctx, d):
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal((3, 3000)).astype(np.float32)
+    cols = [0, 1, 2][:d]
+    for hv in (1e-6, 50.0):
+        h = [hv] * d
+        p = ctx.combined_densities(x, None, cols, h)
+        assert rel_err(p, O.density_fp64(O.repack(x, cols), h)) < REL
+
+
+@pytest.mark.parametrize("d", [1, 2, 3])
+def test_support_counts_exact(ctx, d):
+    rng = np.random.default_rng(40 + d)
+    n = 1500
+    x = rng.standard_normal((3, n)).astype(np.float32)
+    h = np.array([0.3, 0.4, 0.5][:d], np.float32)
+    cols = [0, 1, 2][:d]
+    c = ctx.support_counts(x, None, cols, h)
+    # brute force with the kernel's own float32 test fma(d, d, -1) <= 0 on
+    # centred, 1/h-scaled coordinates is what the GPU counts; away from the
+    # boundary this equals |x_i - x_k| <= h in exact arithmetic
+    y = [(x[c_] - 0.5 * (x[c_].min() + x[c_].max())) * np.float32(1.0 / h[j])
+         for j, c_ in enumerate(cols)]
+    inside = np.ones((n, n), bool)
+    for yy in y:
+        dd = (yy[:, None] - yy[None, :]).astype(np.float64)
+        inside &= dd * dd <= 1.0
+    assert np.array_equal(c, inside.sum(1).astype(np.float64))
+
+
+def test_device_pointer_form(ctx):
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(2)
+    x = rng.standard_normal((2, 5000)).astype(np.float32)
+    dx = torch.from_numpy(x).cuda()
+    dout = torch.empty(5000, dtype=torch.float64, device="cuda")
+    n = ctx.combined_densities_device(dx.data_ptr(), 5000, 2, [0, 1], [0.3, 0.3], None,
+                                      dout.data_ptr())
+    torch.cuda.synchronize()
+    assert n == 5000
+    p = dout.cpu().numpy()
+    assert rel_err(p, ctx.combined_densities(x, None, [0, 1], [0.3, 0.3])) < 1e-12
+
+
+def test_errors_are_status_codes(ctx):
+    x = np.zeros((2, 10), np.float32)
+    with pytest.raises(NativeError) as e:
+        ctx.combined_densities(x, None, [], [])
+    assert e.value.status == 1
+    with pytest.raises(NativeError) as e:
+        ctx.combined_densities(x, None, [0, 1, 0, 1], [1, 1, 1, 1])
+    assert e.value.status == 1
+    with pytest.raises(NativeError) as e:
+        ctx.combined_densities(x, None, [0], [1.0, 2.0])
+    assert e.value.status == 2
+    with pytest.raises(NativeError) as e:
+        ctx.combined_densities(x, None, [0], [-1.0])
+    assert e.value.status == 4
+    with pytest.raises(NativeError) as e:
+        ctx.combined_densities(x, None, [5], [1.0])
+    assert e.value.status == 4
+    with pytest.raises(NativeError) as e:
+        ctx.combined_densities(x, None, [0], [1.0], [10])
+    assert e.value.status == 4
+    y = x.copy()
+    y[0, 3] = np.nan
+    with pytest.raises(NativeError) as e:
+        ctx.combined_densities(y, None, [0], [1.0])
+    assert e.value.status == 5
+    # the context stays usable after errors
+    assert ctx.combined_densities(x + 1, None, [0], [1.0]).shape == (10,)
+
+
+def test_config1_full_size(ctx):
+    x = workloads.gmm_1d(20_000, seed=42)[None]
+    p = ctx.combined_densities(x, None, [0], [0.1])
+    f = O.density_fp64(x, [0.1])
+    assert rel_err(p, f) < REL
+    H = -np.mean(np.log(p))
+    Hf = -np.mean(np.log(f))
+    assert abs(H - Hf) < 1e-6
+
+
+def test_mi_config_pair_sampled(ctx):
+    x = workloads.mi_coords(100_000, 8, seed=2024)
+    h = workloads.scott_bandwidth(x, 2)
+    p = ctx.combined_densities(x, None, [2, 5], [h[2], h[5]])
+    t = np.random.default_rng(0).choice(100_000, 3000, replace=False)
+    f = O.density_fp64(O.repack(x, [2, 5]), [h[2], h[5]], targets=t)
+    assert rel_err(p[t], f) < REL
