@@ -49,6 +49,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--coords", type=int, default=N_COORDS,
+                    help="coordinates of the MI batch (64 = the benchmark workload; "
+                         "smaller values give the small case used for ncu captures)")
     return ap.parse_args()
 
 
@@ -183,8 +186,10 @@ def main():
     args = parse()
     ws, rank, local = dist_env()
     from entropical_gb300 import workloads
-    x = workloads.mi_coords(N_FRAMES, N_COORDS, seed=2024)
+    x = workloads.mi_coords(N_FRAMES, N_COORDS, seed=2024)[: args.coords]
+    x = np.ascontiguousarray(x)
     h = workloads.scott_bandwidth(x, 2)
+    M = x.shape[0]
     if args.impl == "reference":
         return reference_arm(args, x, h)
 
@@ -206,16 +211,16 @@ def main():
     n_sms = torch.cuda.get_device_properties(local).multi_processor_count
     dx = torch.from_numpy(x).cuda(local)
     ptr = dx.data_ptr()
-    iu = np.triu_indices(N_COORDS, 1)
+    iu = np.triu_indices(M, 1)
 
     # work units of the step: in-support (target, source) pairs (untimed)
-    cnt, c1 = ctx.mi_all_pairs_device(ptr, N_FRAMES, N_COORDS, h, counts=True)
+    cnt, c1 = ctx.mi_all_pairs_device(ptr, N_FRAMES, M, h, counts=True)
     support_2d = float(cnt[iu].sum())
     support_1d = float(c1.sum())
     support = support_2d + support_1d
 
     for _ in range(args.warmup):
-        mi, hx = ctx.mi_all_pairs_device(ptr, N_FRAMES, N_COORDS, h)
+        mi, hx = ctx.mi_all_pairs_device(ptr, N_FRAMES, M, h)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
 
     step_ms, k2_ms, k2_pairs, k1_ms, launches = [], [], [], [], 0
@@ -225,7 +230,7 @@ def main():
         for _ in range(args.steps):
             flush.zero_()  # L2 flush between steps (256 MB > 129 MB L2)
             torch.cuda.synchronize()
-            mi, hx = ctx.mi_all_pairs_device(ptr, N_FRAMES, N_COORDS, h)
+            mi, hx = ctx.mi_all_pairs_device(ptr, N_FRAMES, M, h)
             st = ctx.last_stats()
             step_ms.append(st.total_ms)
             k2_ms.append(st.pair_kernel_ms_by_dim[1])
@@ -266,8 +271,9 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n_frames": N_FRAMES, "n_coords": N_COORDS,
-                   "densities_per_step": N_COORDS + len(iu[0]), "l2": "flushed (256 MB write) "
+        "config": {"workload": WORKLOAD if M == N_COORDS else f"{WORKLOAD} (first {M} coords)",
+                   "n_frames": N_FRAMES, "n_coords": M,
+                   "densities_per_step": M + len(iu[0]), "l2": "flushed (256 MB write) "
                    "between steps", "parallelism": "replicas" if ws > 1 else "single GPU"},
         "mi_estimates_per_s": len(iu[0]) * ws / (ms / 1e3),
         "support_pairs_per_step": support,

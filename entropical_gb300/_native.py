@@ -59,7 +59,24 @@ SIGNATURES: dict[str, tuple] = {
     "ent_mi_all_pairs_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t,
                                           c_f32_p, C.c_uint32, c_f64_p, c_f64_p]),
     "ent_entropy_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_uint32, c_f64_p]),
+    "ent_epa_convolution": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_float, c_f32_p]),
+    "ent_hestimate": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, c_u32_p,
+                                C.c_size_t, C.c_uint32, c_f32_p, C.c_uint32, c_f32_p,
+                                C.c_void_p]),
+    "ent_hestimate_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, c_u32_p,
+                                       C.c_size_t, C.c_uint32, c_f32_p, C.c_uint32, c_f32_p,
+                                       C.c_void_p]),
 }
+
+
+class HestStats(C.Structure):
+    """ent_hest_stats: per-column bandwidth-search statistics."""
+    _fields_ = [
+        ("h0", C.c_float),
+        ("conv_evals", C.c_uint32),
+        ("levels_skipped", C.c_uint32),
+        ("warm_converged", C.c_uint32),
+    ]
 
 
 class Instance(C.Structure):

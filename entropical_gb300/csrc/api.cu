@@ -173,6 +173,63 @@ int bits_for(uint32_t max_key) {
 
 }  // namespace
 
+int sort_views(Ctx& c, const std::vector<ViewSpec>& views, SortedViews* out) {
+  cudaError_t e;
+  const cudaStream_t st = c.stream;
+  const uint32_t nv = (uint32_t)views.size();
+  std::vector<ViewDev> hv(nv);
+  out->max_n = 0;
+  out->off.assign(nv, 0);
+  uint64_t vtot = 0;
+  for (uint32_t v = 0; v < nv; ++v) {
+    hv[v].x = views[v].x;
+    hv[v].n = views[v].n;
+    hv[v].pad = 0;
+    out->off[v] = vtot;
+    vtot += views[v].n;
+    out->max_n = std::max(out->max_n, views[v].n);
+  }
+  ViewDev* dv = arena_upload(c, hv, &e);
+  if (e != cudaSuccess) return c.cuda_fail(e, "upload views");
+  ViewStats* dstats = static_cast<ViewStats*>(c.arena.alloc(sizeof(ViewStats) * nv));
+  if (!dstats) return c.fail(ENT_ERR_CUDA, "out of device memory");
+  e = launch_colstats(st, dv, nv, dstats);
+  if (e != cudaSuccess) return c.cuda_fail(e, "colstats");
+  c.stats.kernel_launches += 1;
+  out->stats.assign(nv, ViewStats{});
+  uint64_t* dvoff = arena_upload(c, out->off, &e);
+  if (e != cudaSuccess) return c.cuda_fail(e, "upload view offsets");
+  uint32_t* vk = static_cast<uint32_t*>(c.arena.alloc(4 * vtot));
+  uint32_t* vvals = static_cast<uint32_t*>(c.arena.alloc(4 * vtot));
+  uint32_t* vk2 = static_cast<uint32_t*>(c.arena.alloc(4 * vtot));
+  uint32_t* vv2 = static_cast<uint32_t*>(c.arena.alloc(4 * vtot));
+  if (!vk || !vvals || !vk2 || !vv2) return c.fail(ENT_ERR_CUDA, "out of device memory");
+  e = launch_view_keys(st, dv, dvoff, nv, out->max_n, vk, vvals);
+  if (e != cudaSuccess) return c.cuda_fail(e, "view keys");
+  c.stats.kernel_launches += 1;
+  {
+    SegBuild sb;
+    for (uint32_t v = 0; v < nv; ++v) sb.add(out->off[v], views[v].n);
+    SegTableDev t;
+    int s = sb.upload(c, &t);
+    if (s) return s;
+    e = seg_radix_sort(st, t, nv, sb.total_blocks, vk, vvals, vk2, vv2, 0, 32);
+    if (e != cudaSuccess) return c.cuda_fail(e, "view sort");
+    c.stats.kernel_launches += 12;
+  }
+  // the statistics are needed on the host to plan cell grids
+  e = cudaMemcpyAsync(out->stats.data(), dstats, sizeof(ViewStats) * nv,
+                      cudaMemcpyDeviceToHost, st);
+  if (e != cudaSuccess) return c.cuda_fail(e, "read stats");
+  e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return c.cuda_fail(e, "colstats/sort");
+  for (uint32_t v = 0; v < nv; ++v)
+    if (out->stats[v].nonfinite)
+      return c.fail(ENT_ERR_NONFINITE, "non-finite coordinate in the selection");
+  out->perm = vvals;
+  return ENT_OK;
+}
+
 int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
                 std::vector<InstSpec>& insts, uint32_t mode, EngineOut* out) {
   cudaError_t e;
@@ -183,57 +240,13 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
   if (nv > 65535 || ni > 65535)
     return c.fail(ENT_ERR_TOO_LARGE, "more than 65535 views or instances in one batch");
 
-  // 1. column statistics (one host round trip)
-  std::vector<ViewDev> hv(nv);
-  uint32_t max_vn = 0;
-  std::vector<uint64_t> voff(nv);
-  uint64_t vtot = 0;
-  for (uint32_t v = 0; v < nv; ++v) {
-    hv[v].x = views[v].x;
-    hv[v].n = views[v].n;
-    hv[v].pad = 0;
-    voff[v] = vtot;
-    vtot += views[v].n;
-    max_vn = std::max(max_vn, views[v].n);
-  }
-  ViewDev* dv = arena_upload(c, hv, &e);
-  if (e != cudaSuccess) return c.cuda_fail(e, "upload views");
-  ViewStats* dstats = static_cast<ViewStats*>(c.arena.alloc(sizeof(ViewStats) * nv));
-  if (!dstats) return c.fail(ENT_ERR_CUDA, "out of device memory");
-  e = launch_colstats(st, dv, nv, dstats);
-  if (e != cudaSuccess) return c.cuda_fail(e, "colstats");
-  c.stats.kernel_launches += 1;
-  std::vector<ViewStats> vs(nv);
-  e = cudaMemcpyAsync(vs.data(), dstats, sizeof(ViewStats) * nv,
-                      cudaMemcpyDeviceToHost, st);
-  if (e != cudaSuccess) return c.cuda_fail(e, "read stats");
-
-  // 2. value sort of every view (overlaps the stats read-back)
-  uint64_t* dvoff = arena_upload(c, voff, &e);
-  if (e != cudaSuccess) return c.cuda_fail(e, "upload view offsets");
-  uint32_t* vk = static_cast<uint32_t*>(c.arena.alloc(4 * vtot));
-  uint32_t* vvals = static_cast<uint32_t*>(c.arena.alloc(4 * vtot));
-  uint32_t* vk2 = static_cast<uint32_t*>(c.arena.alloc(4 * vtot));
-  uint32_t* vv2 = static_cast<uint32_t*>(c.arena.alloc(4 * vtot));
-  if (!vk || !vvals || !vk2 || !vv2) return c.fail(ENT_ERR_CUDA, "out of device memory");
-  e = launch_view_keys(st, dv, dvoff, nv, max_vn, vk, vvals);
-  if (e != cudaSuccess) return c.cuda_fail(e, "view keys");
-  c.stats.kernel_launches += 1;
-  {
-    SegBuild sb;
-    for (uint32_t v = 0; v < nv; ++v) sb.add(voff[v], views[v].n);
-    SegTableDev t;
-    int s = sb.upload(c, &t);
-    if (s) return s;
-    e = seg_radix_sort(st, t, nv, sb.total_blocks, vk, vvals, vk2, vv2, 0, 32);
-    if (e != cudaSuccess) return c.cuda_fail(e, "view sort");
-    c.stats.kernel_launches += 12;
-  }
-  e = cudaStreamSynchronize(st);
-  if (e != cudaSuccess) return c.cuda_fail(e, "colstats/sort");
-  for (uint32_t v = 0; v < nv; ++v)
-    if (vs[v].nonfinite)
-      return c.fail(ENT_ERR_NONFINITE, "non-finite coordinate in the selection");
+  // 1-2. column statistics and value sort of every view
+  SortedViews sv;
+  int rs = sort_views(c, views, &sv);
+  if (rs) return rs;
+  const std::vector<ViewStats>& vs = sv.stats;
+  const std::vector<uint64_t>& voff = sv.off;
+  uint32_t* vvals = sv.perm;
 
   // 3. host plan of every instance
   std::vector<InstDev> hi(ni);
@@ -290,7 +303,7 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
       I.tile_cap = (s.n + I.tt - 1) / I.tt + std::min(I.n_strips, s.n);
       I.tile_base = slot;
       slot += I.tile_cap;
-      I.scale = std::pow(0.75, (double)s.d) / (s.norm * prod_h);
+      I.scale = (mode & DM_COUNT) ? 1.0 : std::pow(0.75, (double)s.d) / (s.norm * prod_h);
       I.out = s.out;
     }
     group_slots[d] = slot - group_base[d];
@@ -425,6 +438,18 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
   c.stats.tiles += n_slots;
   c.pending_pairs = true;
   return ENT_OK;
+}
+
+unsigned Ctx::persistent_grid(uint32_t n_work, const void* kern, int threads, size_t smem) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    per_sm = 1;
+  }
+  uint64_t g = (uint64_t)std::max(per_sm, 1) * (uint64_t)n_sms;
+  g = std::min<uint64_t>(g, std::max<uint32_t>(n_work, 1));
+  return (unsigned)g;
 }
 
 void Ctx::collect_kernel_stats() {

@@ -40,6 +40,8 @@ struct Ctx {
   bool pending_pairs = false;
   uint32_t strip_subdiv = 2;  // cells per bandwidth along dimension 1 (d = 2)
 
+  // grid of a persistent kernel: resident CTAs per SM x SMs, capped by work
+  unsigned persistent_grid(uint32_t n_work, const void* kern, int threads, size_t smem);
   int fail(int status, const std::string& msg);
   int cuda_fail(cudaError_t e, const char* where);
   int begin_call();
@@ -63,6 +65,25 @@ struct InstSpec {
   double* out = nullptr;  // device, by original index (nullable)
   uint32_t S = 2;
 };
+
+namespace ent { struct ViewStats; }
+#include "engine.h"
+
+// Column statistics and value order of a set of views (one host sync).
+struct SortedViews {
+  std::vector<ent::ViewStats> stats;
+  std::vector<uint64_t> off;  // element offset of each view in perm
+  uint32_t* perm = nullptr;   // device: per view, sorted local indices
+  uint32_t max_n = 0;
+};
+int sort_views(Ctx& c, const std::vector<ViewSpec>& views, SortedViews* out);
+
+// AMISE convolution / bandwidth search over device columns stored back to
+// back in `raw`. mode 0: convolution at the given bandwidths; 1: full
+// interval search; 2: search warm-started from the given bandwidths.
+int hestimate_engine(Ctx& c, const float* raw, const std::vector<uint64_t>& raw_off,
+                     const std::vector<uint32_t>& lens, int mode, const float* h_fixed_or_init,
+                     int skip, float* h_out, float* conv_out, ent_hest_stats* stats);
 
 struct EngineOut {
   double* d_logsum_sorted = nullptr;  // per instance, in slot order

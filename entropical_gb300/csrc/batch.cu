@@ -45,11 +45,8 @@ int run_entropies(Ctx& c, const std::vector<ViewSpec>& views,
   H->assign(insts.size(), 0.0);
   for (size_t r = 0; r < insts.size(); ++r) {
     const uint32_t i = eo.slot_order[r];
-    // support counts carry the 0.75^d / prod(h) factor of the scale
     if (counts) {
-      double f = std::pow(0.75, (double)insts[i].d);
-      for (uint32_t j = 0; j < insts[i].d; ++j) f /= (double)insts[i].h[j];
-      (*H)[i] = std::round(ls[r] / f);
+      (*H)[i] = ls[r];
     } else {
       (*H)[i] = -ls[r] / (double)insts[i].n;
     }

@@ -1,0 +1,739 @@
+// AMISE convolution sums and the hestimate bandwidth search on the device.
+//
+// Replaces epa_convolution (densities_omp.cpp:235-277; the CUDA form
+// epa_conv.cuh:191-229 launches the density kernel instead, see the
+// reference defect list) and the AmiseMin search (hestimate.cpp:41-104):
+//
+//   C(h) = 1/n^2 sum_i sum_j max(0, 4.5 - 2.25 |x_i - x_j| / h)
+//   amise(h) = (0.04 / h^5 * C(h))^0.2 * 1.25 * 0.6^0.8 / n^0.8
+//   bracket [0.1 h0, 2 h0], prec 0.01 h0: at each level evaluate amise at the
+//   two quarter points and keep the half on the side of the smaller value.
+//
+// Columns are value-sorted once (radix sort of the engine); each target tile
+// of the sorted column sees one contiguous run of sources within 2 h_max,
+// staged into shared memory with TMA bulk copies exactly as in the density
+// kernel. One pass evaluates BOTH pivots of a level (packed f32x2 over the
+// two bandwidths). The per-column search state lives on the device; each
+// level is conv -> per-column reduce -> decide, all columns at once, and the
+// level sequence is captured into one CUDA graph.
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <vector>
+
+#include "../../include/entropical_gb300.h"
+#include "api_internal.h"
+#include "engine.h"
+#include "staging.cuh"
+
+using namespace ent;
+
+namespace {
+
+struct ConvCol {
+  const float* xs;  // sorted, centred column (n + 8 floats)
+  uint32_t n;
+  uint32_t tile_base;
+  uint32_t n_tiles;
+  uint32_t pad;
+};
+
+// Search state of one column (hestimate.cpp:55-86 recursion, unrolled).
+struct HestState {
+  float h0, lo, hi, prec;
+  float glo, ghi;      // global bracket [0.1 h0, 2 h0]
+  float node_lo, node_hi;  // warm start: bracket after the skipped levels
+  float piv[2];        // pivots of the current level (or the single h)
+  float result;
+  int level, done, iter_max;
+  int n_conv;
+  int dirs;            // bit 0: a lower-half decision, bit 1: an upper-half one
+  int warm, converged;
+  uint32_t n;
+};
+
+// Sequential float sums in the reference's order give the reference's h0
+// bit for bit (Boost lazy variance over float, hestimate.cpp:19-30).
+__global__ void k_thumb(const ConvCol* __restrict__ cols, const float* __restrict__ raw,
+                        const uint64_t* __restrict__ raw_off, const double* __restrict__ pw,
+                        HestState* __restrict__ st, uint32_t n_cols) {
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n_cols) return;
+  const float* x = raw + raw_off[c];
+  const uint32_t n = cols[c].n;
+  float s = 0.f, s2 = 0.f;
+  for (uint32_t i = 0; i < n; ++i) {
+    const float v = x[i];
+    s = __fadd_rn(s, v);
+    s2 = __fadd_rn(s2, __fmul_rn(v, v));
+  }
+  const float m2 = __fdiv_rn(s2, (float)n);
+  const float m = __fdiv_rn(s, (float)n);
+  const float var = __fsub_rn(m2, __fmul_rn(m, m));
+  st[c].h0 = (float)(pw[c] * sqrt((double)var));
+  st[c].n = n;
+}
+
+__global__ void k_gather_sorted(const ConvCol* __restrict__ cols,
+                                const float* __restrict__ raw,
+                                const uint64_t* __restrict__ raw_off,
+                                const uint32_t* __restrict__ perm,
+                                const float* __restrict__ center) {
+  const ConvCol& C = cols[blockIdx.y];
+  const float* x = raw + raw_off[blockIdx.y];
+  const uint32_t* p = perm + raw_off[blockIdx.y];
+  float* xs = const_cast<float*>(C.xs);
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < C.n + 8;
+       k += gridDim.x * blockDim.x)
+    xs[k] = k < C.n ? __fsub_rn(x[p[k]], center[blockIdx.y]) : 0.f;
+}
+
+__device__ __forceinline__ float piv_of(double a, double b) { return (float)(a + b); }
+
+// Start a full search (hestimate.cpp:101-103) or a warm one: descend
+// `skip` levels of the same dyadic bracket tree towards h_init without
+// evaluating anything, then search from there.
+__global__ void k_hest_init(HestState* __restrict__ st, uint32_t n_cols,
+                            const float* __restrict__ h_init, int skip, int fixed_h) {
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n_cols) return;
+  HestState s = st[c];
+  s.level = 0;
+  s.done = 0;
+  s.n_conv = 0;
+  s.dirs = 0;
+  s.iter_max = 20;
+  s.converged = 1;
+  s.warm = 0;
+  if (fixed_h) {  // plain epa_convolution: one bandwidth, no search
+    s.piv[0] = s.piv[1] = h_init[c];
+    st[c] = s;
+    return;
+  }
+  s.prec = (float)(0.01 * (double)s.h0);
+  s.lo = (float)(0.1 * (double)s.h0);
+  s.hi = 2.f * s.h0;
+  s.glo = s.lo;
+  s.ghi = s.hi;
+  if (h_init && skip > 0) {
+    s.warm = 1;
+    const float t = h_init[c];
+    for (int k = 0; k < skip; ++k) {
+      const float delta = s.hi - s.lo;
+      const float pivot = (float)((double)s.lo + 0.5 * (double)delta);
+      if (s.iter_max == 0 || delta <= s.prec) break;
+      if (t < pivot) s.hi = pivot; else s.lo = pivot;
+      s.iter_max -= 1;
+      s.level += 1;
+    }
+  }
+  s.node_lo = s.lo;
+  s.node_hi = s.hi;
+  const float delta = s.hi - s.lo;
+  const float pivot = (float)((double)s.lo + 0.5 * (double)delta);
+  if (s.iter_max == 0 || delta <= s.prec) {
+    s.done = 1;
+    s.result = pivot;
+  } else {
+    s.piv[0] = (float)((double)pivot - 0.25 * (double)delta);
+    s.piv[1] = (float)((double)pivot + 0.25 * (double)delta);
+  }
+  st[c] = s;
+}
+
+__global__ void k_conv_plan(const ConvCol* __restrict__ cols, uint32_t n_cols,
+                            const uint32_t* __restrict__ col_tile_base,
+                            const HestState* __restrict__ st, int fixed_h,
+                            TileDesc* __restrict__ tiles, uint32_t n_slots, uint32_t tt) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n_slots) return;
+  uint32_t lo = 0, hi = n_cols;
+  while (hi - lo > 1) {
+    const uint32_t m = (lo + hi) / 2;
+    if (col_tile_base[m] <= g) lo = m; else hi = m;
+  }
+  const ConvCol& C = cols[lo];
+  TileDesc td;
+  td.inst = lo;
+  td.n_runs = 0;
+  td.t_count = 0;
+  td.t_begin = 0;
+  const uint32_t t = g - C.tile_base;
+  if (t < C.n_tiles) {
+    const uint32_t tb = t * tt;
+    const uint32_t tc = min(tt, C.n - tb);
+    // widest support any level of the search can ask for: 2 * (2 h0)
+    const float hmax = fixed_h ? st[lo].piv[0] : st[lo].ghi;
+    const float w = 2.f * hmax * (1.f + 1e-5f) + 1e-30f;
+    const float xf = C.xs[tb], xl = C.xs[tb + tc - 1];
+    const float eps = 1e-6f * (fabsf(xf) + fabsf(xl));
+    const float vlo = xf - w - eps, vhi = xl + w + eps;
+    uint32_t a = 0, b = C.n;
+    while (a < b) {
+      const uint32_t m = a + (b - a) / 2;
+      if (C.xs[m] < vlo) a = m + 1; else b = m;
+    }
+    uint32_t e = a, f = C.n;
+    while (e < f) {
+      const uint32_t m = e + (f - e) / 2;
+      if (C.xs[m] <= vhi) e = m + 1; else f = m;
+    }
+    td.t_begin = tb;
+    td.t_count = tc;
+    td.n_runs = 1;
+    td.lo[0] = a;
+    td.len[0] = e - a;
+  }
+  tiles[g] = td;
+}
+
+// One pass over (target, source) pairs within the window evaluates the
+// convolution kernel at NP bandwidths (NP = 1: plain epa_convolution,
+// NP = 2: both pivots of a search level).
+template <int NP, int R>
+__global__ void __launch_bounds__(128)
+    k_conv(const TileDesc* __restrict__ tiles, uint32_t n_slots,
+           const ConvCol* __restrict__ cols, const HestState* __restrict__ st,
+           uint32_t* work_counter, uint32_t* err, double* __restrict__ tile_sum) {
+  typedef Cfg<1, R> CC;
+  extern __shared__ __align__(128) unsigned char dsm[];
+  float* bufs = reinterpret_cast<float*>(dsm);
+  __shared__ __align__(8) uint64_t full[2];
+  __shared__ Piece ptab[2][CC::MAXP];
+  __shared__ uint32_t npc[2];
+  __shared__ uint32_t run_lo[MAX_RUNS], run_pre[MAX_RUNS + 1];
+  __shared__ uint32_t s_g, s_nr, s_tb, s_tc, s_col, s_skip;
+  __shared__ double s_part[CC::NW][2];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) {
+    mbar_init(&full[0], 1);
+    mbar_init(&full[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  uint32_t q = 0;
+  for (;;) {
+    if (tid == 0) {
+      const uint32_t g = atomicAdd(work_counter, 1u);
+      s_g = g;
+      if (g < n_slots) {
+        const TileDesc* T = tiles + g;
+        s_tb = T->t_begin;
+        s_tc = T->t_count;
+        s_col = T->inst;
+        s_nr = T->n_runs;
+        s_skip = (T->t_count == 0 || st[T->inst].done) ? 1u : 0u;
+        run_pre[0] = 0;
+        for (uint32_t r = 0; r < T->n_runs; ++r) {
+          run_lo[r] = T->lo[r];
+          run_pre[r + 1] = run_pre[r] + T->len[r];
+        }
+      }
+    }
+    __syncthreads();
+    const uint32_t g = s_g;
+    if (g >= n_slots) break;
+    if (s_skip) {
+      if (tid == 0) {
+        tile_sum[2 * (size_t)g] = 0.0;
+        tile_sum[2 * (size_t)g + 1] = 0.0;
+      }
+      __syncthreads();
+      continue;
+    }
+    const uint32_t tc = s_tc, tb = s_tb, nr = s_nr, nsrc = run_pre[nr];
+    const ConvCol& Cc = cols[s_col];
+    const float* __restrict__ xs = Cc.xs;
+    const uint32_t nch = (nsrc + CC::CH - 1) / CC::CH;
+    if (tid == 0 && nch > 0)
+      issue_chunk<1, R>(0, q & 1u, nsrc, nr, run_lo, run_pre, xs, bufs, ptab, npc, full);
+    float coef[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) coef[k] = -2.25f / st[s_col].piv[k];
+    float T[R];
+    float ks[NP][R], kc[NP][R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const uint32_t li = warp * R + r;
+      T[r] = li < tc ? xs[tb + li] : 1e30f;
+#pragma unroll
+      for (int k = 0; k < NP; ++k) ks[k][r] = kc[k][r] = 0.f;
+    }
+    bool aborted = false;
+    uint32_t ab_q = 0;
+    bool ab_next = false;
+    for (uint32_t c = 0; c < nch; ++c) {
+      const uint32_t qq = q + c, b = qq & 1u;
+      if (tid == 0 && c + 1 < nch)
+        issue_chunk<1, R>(c + 1, (qq + 1) & 1u, nsrc, nr, run_lo, run_pre, xs, bufs, ptab,
+                          npc, full);
+      const bool ok = mbar_wait(&full[b], (qq >> 1) & 1u);
+      if (ok) {
+        const float* B = bufs + (size_t)b * CC::CAP;
+        for (uint32_t pi = 0; pi < npc[b]; ++pi) {
+          const uint32_t s0 = ptab[b][pi].s0, n = ptab[b][pi].n;
+          if constexpr (NP == 1) {
+            float acc[R];
+#pragma unroll
+            for (int r = 0; r < R; ++r) acc[r] = 0.f;
+#pragma unroll 2
+            for (uint32_t k = lane; k < n; k += 32) {
+              const float s = B[s0 + k];
+#pragma unroll
+              for (int r = 0; r < R; ++r) {
+                const float t = fabsf(T[r] - s);
+                acc[r] += fmaxf(fmaf(t, coef[0], 4.5f), 0.f);
+              }
+            }
+#pragma unroll
+            for (int r = 0; r < R; ++r) kahan_add(ks[0][r], kc[0][r], acc[r]);
+          } else {
+            const f32x2 CO = pk2(coef[0], coef[1]);
+            const f32x2 F45 = pk2(4.5f, 4.5f);
+            f32x2 acc[R];
+#pragma unroll
+            for (int r = 0; r < R; ++r) acc[r] = pk2(0.f, 0.f);
+#pragma unroll 2
+            for (uint32_t k = lane; k < n; k += 32) {
+              const float s = B[s0 + k];
+#pragma unroll
+              for (int r = 0; r < R; ++r) {
+                const float t = fabsf(T[r] - s);
+                const f32x2 w = fma2(pk2(t, t), CO, F45);
+                float w0, w1;
+                upk2(w, w0, w1);
+                acc[r] = add2(acc[r], pk2(fmaxf(w0, 0.f), fmaxf(w1, 0.f)));
+              }
+            }
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+              float a0, a1;
+              upk2(acc[r], a0, a1);
+              kahan_add(ks[0][r], kc[0][r], a0);
+              kahan_add(ks[1][r], kc[1][r], a1);
+            }
+          }
+        }
+      }
+      if (__syncthreads_or(!ok)) {
+        aborted = true;
+        ab_q = qq;
+        ab_next = c + 1 < nch;
+        break;
+      }
+    }
+    if (aborted) {
+      if (tid == 0) {
+        atomicOr(err, EF_TIMEOUT);
+        mbar_wait(&full[ab_q & 1u], (ab_q >> 1) & 1u);
+        if (ab_next) mbar_wait(&full[(ab_q + 1) & 1u], ((ab_q + 1) >> 1) & 1u);
+      }
+      __syncthreads();
+      return;
+    }
+    q += nch;
+    const int tgt = lane >> (5 - Log2<R>::v);
+    const bool writer = (lane & ((32 / R) - 1)) == 0;
+    const uint32_t li = warp * R + tgt;
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+      float v[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[r] = ks[k][r] - kc[k][r];
+      const float tot = warp_transpose_sum<R>(v, lane);
+      double part = (writer && li < tc) ? (double)tot : 0.0;
+      for (int o = 16; o; o >>= 1) part += __shfl_xor_sync(FULL_MASK, part, o);
+      if (lane == 0) s_part[warp][k] = part;
+    }
+    __syncthreads();
+    if (tid == 0) {
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        double t = 0.0;
+        if (k < NP)
+          for (int w = 0; w < CC::NW; ++w) t += s_part[w][k];
+        tile_sum[2 * (size_t)g + k] = t;
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    k_conv_reduce(const ConvCol* __restrict__ cols, const double* __restrict__ tile_sum,
+                  double* __restrict__ col_sum) {
+  __shared__ double sw[8][2];
+  const ConvCol& C = cols[blockIdx.x];
+  double a0 = 0.0, a1 = 0.0;
+  for (uint32_t t = threadIdx.x; t < C.n_tiles; t += blockDim.x) {
+    a0 += tile_sum[2 * (size_t)(C.tile_base + t)];
+    a1 += tile_sum[2 * (size_t)(C.tile_base + t) + 1];
+  }
+  for (int o = 16; o; o >>= 1) {
+    a0 += __shfl_xor_sync(FULL_MASK, a0, o);
+    a1 += __shfl_xor_sync(FULL_MASK, a1, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    sw[threadIdx.x >> 5][0] = a0;
+    sw[threadIdx.x >> 5][1] = a1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t0 = 0.0, t1 = 0.0;
+    for (int w = 0; w < 8; ++w) {
+      t0 += sw[w][0];
+      t1 += sw[w][1];
+    }
+    col_sum[2 * blockIdx.x] = t0;
+    col_sum[2 * blockIdx.x + 1] = t1;
+  }
+}
+
+// AmiseMin::_amise (hestimate.cpp:41-53) in the reference's float/double mix.
+__device__ float amise_of(float conv, float h, uint32_t n) {
+  float a = (float)(0.04 * 1 / pow((double)h, 5.0) * (double)conv);
+  a = (float)pow((double)a, 0.2);
+  a = (float)((double)a * 1.25 * pow(0.6, 0.8) / pow((double)(float)n, 0.8));
+  return a;
+}
+
+__device__ __forceinline__ float conv_value(double sum, uint32_t n) {
+  // kahan_sum(outer) / (n_rows * n_rows) in float (densities_omp.cpp:276)
+  return __fdiv_rn((float)sum, (float)((unsigned long long)n * n));
+}
+
+// One level of the interval search (hestimate.cpp:55-86) for every column.
+__global__ void k_hest_level(HestState* __restrict__ st, uint32_t n_cols,
+                             const double* __restrict__ col_sum,
+                             float* __restrict__ conv_out) {
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n_cols) return;
+  HestState s = st[c];
+  if (s.done) return;
+  const float cl = conv_value(col_sum[2 * c], s.n);
+  const float ch = conv_value(col_sum[2 * c + 1], s.n);
+  if (conv_out) {
+    conv_out[2 * c] = cl;
+    conv_out[2 * c + 1] = ch;
+  }
+  const float al = amise_of(cl, s.piv[0], s.n);
+  const float ah = amise_of(ch, s.piv[1], s.n);
+  s.n_conv += 2;
+  const float delta0 = s.hi - s.lo;
+  const float pivot0 = (float)((double)s.lo + 0.5 * (double)delta0);
+  if (al < ah) {
+    s.hi = pivot0;
+    s.dirs |= 1;
+  } else {
+    s.lo = pivot0;
+    s.dirs |= 2;
+  }
+  s.iter_max -= 1;
+  s.level += 1;
+  const float delta = s.hi - s.lo;
+  const float pivot = (float)((double)s.lo + 0.5 * (double)delta);
+  if (s.iter_max == 0 || delta <= s.prec) {
+    s.done = 1;
+    s.result = pivot;
+    // A warm search whose every decision pointed towards the same edge of
+    // its starting node, where that edge is not the global bracket's, may
+    // have left the optimum outside the node: report it for a full search.
+    if (s.warm) {
+      if ((s.dirs == 2 && s.node_hi < s.ghi) || (s.dirs == 1 && s.node_lo > s.glo))
+        s.converged = 0;
+    }
+  } else {
+    s.piv[0] = (float)((double)pivot - 0.25 * (double)delta);
+    s.piv[1] = (float)((double)pivot + 0.25 * (double)delta);
+  }
+  st[c] = s;
+}
+
+__global__ void k_conv_single_out(const HestState* __restrict__ st, uint32_t n_cols,
+                                  const double* __restrict__ col_sum, float* __restrict__ out) {
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < n_cols) out[c] = conv_value(col_sum[2 * c], st[c].n);
+}
+
+template <class T>
+T* upload(Ctx& c, const std::vector<T>& v, cudaError_t* e) {
+  T* p = static_cast<T*>(c.arena.alloc(sizeof(T) * std::max<size_t>(v.size(), 1)));
+  if (!p) {
+    *e = cudaErrorMemoryAllocation;
+    return nullptr;
+  }
+  *e = v.empty() ? cudaSuccess
+                 : cudaMemcpyAsync(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice,
+                                   c.stream);
+  return p;
+}
+
+template <int NP, int R>
+cudaError_t launch_conv_t(cudaStream_t s, const TileDesc* tiles, uint32_t n_slots,
+                          const ConvCol* cols, const HestState* st, uint32_t* wc,
+                          uint32_t* err, double* tile_sum, int n_sms) {
+  typedef Cfg<1, R> CC;
+  auto kern = k_conv<NP, R>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)CC::SMEM);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, CC::NT, CC::SMEM);
+  if (e != cudaSuccess) return e;
+  uint64_t grid = (uint64_t)std::max(per_sm, 1) * (uint64_t)n_sms;
+  grid = std::min<uint64_t>(grid, std::max<uint32_t>(n_slots, 1));
+  e = cudaMemsetAsync(wc, 0, sizeof(uint32_t), s);
+  if (e != cudaSuccess) return e;
+  kern<<<(unsigned)grid, CC::NT, CC::SMEM, s>>>(tiles, n_slots, cols, st, wc, err, tile_sum);
+  return cudaGetLastError();
+}
+
+constexpr int CONV_R1 = 16, CONV_R2 = 8;
+
+}  // namespace
+
+// Shared implementation of ent_epa_convolution / ent_hestimate. `raw` holds
+// n_cols device columns back to back (raw_off offsets). mode: 0 = fixed
+// bandwidths h_fixed (convolution only), 1 = full search, 2 = warm search.
+int hestimate_engine(Ctx& c, const float* raw, const std::vector<uint64_t>& raw_off,
+                     const std::vector<uint32_t>& lens, int mode, const float* h_fixed_or_init,
+                     int skip, float* h_out, float* conv_out, ent_hest_stats* stats) {
+  cudaError_t e;
+  const cudaStream_t s = c.stream;
+  const uint32_t nc = (uint32_t)lens.size();
+  if (nc == 0) return ENT_OK;
+  // value sort of every column through the engine's radix sort
+  std::vector<ViewSpec> views(nc);
+  for (uint32_t i = 0; i < nc; ++i) views[i] = {raw + raw_off[i], lens[i]};
+  SortedViews sv;
+  int rs = sort_views(c, views, &sv);
+  if (rs) return rs;
+  std::vector<ConvCol> hc(nc);
+  const uint32_t tt_used = mode == 0 ? Cfg<1, CONV_R1>::TT : Cfg<1, CONV_R2>::TT;
+  uint32_t slots = 0;
+  std::vector<uint32_t> base(nc);
+  std::vector<float> center(nc);
+  std::vector<double> pw(nc);
+  for (uint32_t i = 0; i < nc; ++i) {
+    hc[i].n = lens[i];
+    hc[i].xs = static_cast<float*>(c.arena.alloc(4 * ((size_t)lens[i] + 8)));
+    if (!hc[i].xs) return c.fail(ENT_ERR_CUDA, "out of device memory");
+    hc[i].n_tiles = (lens[i] + tt_used - 1) / tt_used;
+    hc[i].tile_base = slots;
+    base[i] = slots;
+    slots += hc[i].n_tiles;
+    center[i] = 0.5f * (sv.stats[i].mn + sv.stats[i].mx);
+    pw[i] = std::pow((double)lens[i], -1.0 / 7.0);  // std::pow(n_rows, -1/7)
+  }
+  ConvCol* dcols = upload(c, hc, &e);
+  if (e != cudaSuccess) return c.cuda_fail(e, "upload columns");
+  uint64_t* doff = upload(c, raw_off, &e);
+  if (e != cudaSuccess) return c.cuda_fail(e, "upload offsets");
+  float* dcenter = upload(c, center, &e);
+  if (e != cudaSuccess) return c.cuda_fail(e, "upload centres");
+  double* dpw = upload(c, pw, &e);
+  if (e != cudaSuccess) return c.cuda_fail(e, "upload powers");
+  uint32_t* dbase = upload(c, base, &e);
+  if (e != cudaSuccess) return c.cuda_fail(e, "upload tile bases");
+  std::vector<float> hin(nc, 1.f);
+  if (h_fixed_or_init) hin.assign(h_fixed_or_init, h_fixed_or_init + nc);
+  float* dhin = upload(c, hin, &e);
+  if (e != cudaSuccess) return c.cuda_fail(e, "upload bandwidths");
+  HestState* dst = static_cast<HestState*>(c.arena.alloc(sizeof(HestState) * nc));
+  TileDesc* tiles = static_cast<TileDesc*>(c.arena.alloc(sizeof(TileDesc) * std::max(slots, 1u)));
+  double* tsum = static_cast<double*>(c.arena.alloc(16 * (size_t)std::max(slots, 1u)));
+  double* csum = static_cast<double*>(c.arena.alloc(16 * (size_t)nc));
+  uint32_t* wc = static_cast<uint32_t*>(c.arena.alloc(16));
+  float* dconv = static_cast<float*>(c.arena.alloc(8 * (size_t)nc * 24));
+  if (!dst || !tiles || !tsum || !csum || !wc || !dconv)
+    return c.fail(ENT_ERR_CUDA, "out of device memory");
+  cudaMemsetAsync(dst, 0, sizeof(HestState) * nc, s);
+
+  const unsigned gx = std::min<uint32_t>((std::max(sv.max_n, 1u) + 255) / 256 + 1, 1024);
+  k_gather_sorted<<<dim3(gx, nc), 256, 0, s>>>(dcols, raw, doff, sv.perm, dcenter);
+  k_thumb<<<(nc + 63) / 64, 64, 0, s>>>(dcols, raw, doff, dpw, dst, nc);
+  k_hest_init<<<(nc + 63) / 64, 64, 0, s>>>(dst, nc, (mode == 0 || mode == 2) ? dhin : nullptr,
+                                            mode == 2 ? skip : 0, mode == 0 ? 1 : 0);
+  k_conv_plan<<<(std::max(slots, 1u) + 127) / 128, 128, 0, s>>>(dcols, nc, dbase, dst,
+                                                                 mode == 0 ? 1 : 0, tiles, slots,
+                                                                 tt_used);
+  c.stats.kernel_launches += 4;
+  if ((e = cudaGetLastError()) != cudaSuccess) return c.cuda_fail(e, "hestimate setup");
+
+  cudaEventRecord(c.ev_k0, s);
+  if (mode == 0) {
+    e = launch_conv_t<1, CONV_R1>(s, tiles, slots, dcols, dst, wc, c.d_err, tsum, c.n_sms);
+    if (e != cudaSuccess) return c.cuda_fail(e, "convolution kernel");
+    k_conv_reduce<<<nc, 256, 0, s>>>(dcols, tsum, csum);
+    k_conv_single_out<<<(nc + 63) / 64, 64, 0, s>>>(dst, nc, csum, dconv);
+    c.stats.kernel_launches += 3;
+  } else {
+    // The level loop (at most 20 levels; 8 for every finite h0 > 0) runs as
+    // one captured CUDA graph of conv -> reduce -> decide per level.
+    const int max_levels = 9 - (mode == 2 ? std::min(skip, 8) : 0);
+    typedef Cfg<1, CONV_R2> CC;
+    auto kern = k_conv<2, CONV_R2>;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CC::SMEM);
+    if (e != cudaSuccess) return c.cuda_fail(e, "conv attributes");
+    const unsigned grid = c.persistent_grid(slots, (const void*)kern, CC::NT, CC::SMEM);
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return c.cuda_fail(e, "begin capture");
+    for (int L = 0; L < max_levels; ++L) {
+      cudaMemsetAsync(wc, 0, sizeof(uint32_t), s);
+      kern<<<grid, CC::NT, CC::SMEM, s>>>(tiles, slots, dcols, dst, wc, c.d_err, tsum);
+      k_conv_reduce<<<nc, 256, 0, s>>>(dcols, tsum, csum);
+      k_hest_level<<<(nc + 63) / 64, 64, 0, s>>>(dst, nc, csum, dconv + 2 * (size_t)nc * L);
+    }
+    e = cudaStreamEndCapture(s, &graph);
+    if (e != cudaSuccess) return c.cuda_fail(e, "end capture");
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    if (e != cudaSuccess) {
+      cudaGraphDestroy(graph);
+      return c.cuda_fail(e, "graph instantiate");
+    }
+    e = cudaGraphLaunch(exec, s);
+    cudaStreamSynchronize(s);
+    cudaGraphExecDestroy(exec);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return c.cuda_fail(e, "graph launch");
+    c.stats.kernel_launches += 3 * max_levels;
+  }
+  cudaEventRecord(c.ev_k1, s);
+
+  std::vector<HestState> hs(nc);
+  e = cudaMemcpyAsync(hs.data(), dst, sizeof(HestState) * nc, cudaMemcpyDeviceToHost, s);
+  if (e != cudaSuccess) return c.cuda_fail(e, "read search state");
+  if (mode == 0 && conv_out) {
+    e = cudaMemcpyAsync(conv_out, dconv, 4 * (size_t)nc, cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) return c.cuda_fail(e, "read convolution");
+  }
+  e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return c.cuda_fail(e, "hestimate");
+  if (mode != 0) {
+    std::vector<uint32_t> redo;
+    for (uint32_t i = 0; i < nc; ++i) {
+      if (!hs[i].done) return c.fail(ENT_ERR_STATE, "bandwidth search did not finish");
+      h_out[i] = hs[i].result;
+      if (stats) {
+        stats[i].h0 = hs[i].h0;
+        stats[i].conv_evals = (uint32_t)hs[i].n_conv;
+        stats[i].levels_skipped = mode == 2 ? (uint32_t)skip : 0u;
+        stats[i].warm_converged = mode == 2 ? (uint32_t)hs[i].converged : 0u;
+      }
+      if (mode == 2 && !hs[i].converged) redo.push_back(i);
+    }
+    if (!redo.empty()) {
+      // fall back to the full search for the columns the warm start missed
+      std::vector<uint64_t> off2;
+      std::vector<uint32_t> len2;
+      for (uint32_t i : redo) {
+        off2.push_back(raw_off[i]);
+        len2.push_back(lens[i]);
+      }
+      std::vector<float> h2(redo.size());
+      std::vector<ent_hest_stats> st2(redo.size());
+      int r2 = hestimate_engine(c, raw, off2, len2, 1, nullptr, 0, h2.data(), nullptr,
+                                st2.data());
+      if (r2) return r2;
+      for (size_t q = 0; q < redo.size(); ++q) {
+        h_out[redo[q]] = h2[q];
+        if (stats) stats[redo[q]].conv_evals += st2[q].conv_evals;
+      }
+    }
+  }
+  return ENT_OK;
+}
+
+static int hest_common(ent_ctx* ctx, const float* coords, size_t n_rows, size_t n_cols,
+                       const uint32_t* cols, size_t n_sel, uint32_t mode, const float* h_init,
+                       uint32_t skip, float* h_out, ent_hest_stats* stats, bool device_in) {
+  if (!ctx) return ENT_ERR_ARG;
+  Ctx& c = *reinterpret_cast<Ctx*>(ctx);
+  int s = c.begin_call();
+  if (s) return s;
+  if (!coords || !h_out || n_sel == 0) return c.fail(ENT_ERR_ARG, "null argument");
+  if (mode > ENT_HEST_AMISE_WARM) return c.fail(ENT_ERR_ARG, "unknown hestimate mode");
+  if (mode == ENT_HEST_AMISE_WARM && !h_init) return c.fail(ENT_ERR_ARG, "warm start needs h_init");
+  if (n_rows < 2 || n_rows > 0xffffff00ull) return c.fail(ENT_ERR_ARG, "bad row count");
+  std::vector<uint64_t> off(n_sel);
+  std::vector<uint32_t> lens(n_sel, (uint32_t)n_rows);
+  const float* raw = coords;
+  for (size_t q = 0; q < n_sel; ++q) {
+    const uint32_t col = cols ? cols[q] : (uint32_t)q;
+    if (col >= n_cols) return c.fail(ENT_ERR_ARG, "column index out of range");
+    off[q] = (uint64_t)col * n_rows;
+  }
+  if (!device_in) {
+    float* p = static_cast<float*>(c.arena.alloc(4 * n_rows * n_sel));
+    if (!p) return c.fail(ENT_ERR_CUDA, "out of device memory");
+    for (size_t q = 0; q < n_sel; ++q) {
+      cudaError_t e = cudaMemcpyAsync(p + q * n_rows, coords + off[q], 4 * n_rows,
+                                      cudaMemcpyHostToDevice, c.stream);
+      if (e != cudaSuccess) return c.cuda_fail(e, "copy coordinates");
+      off[q] = q * n_rows;
+    }
+    raw = p;
+  }
+  if (mode == ENT_HEST_THUMB) {
+    // h0 only: a zero-level search reports it
+    std::vector<float> dummy(n_sel);
+    std::vector<ent_hest_stats> st(n_sel);
+    s = hestimate_engine(c, raw, off, lens, 2, h_out, 64, dummy.data(), nullptr, st.data());
+    if (s) return s;
+    for (size_t q = 0; q < n_sel; ++q) {
+      h_out[q] = st[q].h0;
+      if (stats) {
+        stats[q] = st[q];
+        stats[q].conv_evals = 0;
+      }
+    }
+  } else {
+    s = hestimate_engine(c, raw, off, lens, (int)mode, h_init, (int)skip, h_out, nullptr, stats);
+    if (s) return s;
+  }
+  s = c.end_call();
+  c.collect_kernel_stats();
+  return s;
+}
+
+extern "C" {
+
+int ent_epa_convolution(ent_ctx* ctx, const float* sorted, size_t n, float h, float* out) {
+  if (!ctx) return ENT_ERR_ARG;
+  Ctx& c = *reinterpret_cast<Ctx*>(ctx);
+  int s = c.begin_call();
+  if (s) return s;
+  if (!sorted || !out || n == 0) return c.fail(ENT_ERR_ARG, "null argument");
+  if (!(h > 0.f) || !std::isfinite(h)) return c.fail(ENT_ERR_ARG, "bandwidth must be finite and positive");
+  if (n > 0xffffff00ull) return c.fail(ENT_ERR_TOO_LARGE, "too many rows");
+  float* p = static_cast<float*>(c.arena.alloc(4 * n));
+  if (!p) return c.fail(ENT_ERR_CUDA, "out of device memory");
+  cudaError_t e = cudaMemcpyAsync(p, sorted, 4 * n, cudaMemcpyHostToDevice, c.stream);
+  if (e != cudaSuccess) return c.cuda_fail(e, "copy coordinates");
+  std::vector<uint64_t> off(1, 0);
+  std::vector<uint32_t> lens(1, (uint32_t)n);
+  float hv = h, dummy = 0.f;
+  s = hestimate_engine(c, p, off, lens, 0, &hv, 0, &dummy, out, nullptr);
+  if (s) return s;
+  s = c.end_call();
+  c.collect_kernel_stats();
+  return s;
+}
+
+int ent_hestimate(ent_ctx* ctx, const float* coords, size_t n_rows, size_t n_cols,
+                  const uint32_t* cols, size_t n_sel, uint32_t mode, const float* h_init,
+                  uint32_t skip_levels, float* h_out, ent_hest_stats* stats) {
+  return hest_common(ctx, coords, n_rows, n_cols, cols, n_sel, mode, h_init, skip_levels,
+                     h_out, stats, false);
+}
+
+int ent_hestimate_device(ent_ctx* ctx, const float* d_coords, size_t n_rows, size_t n_cols,
+                         const uint32_t* cols, size_t n_sel, uint32_t mode,
+                         const float* h_init, uint32_t skip_levels, float* h_out,
+                         ent_hest_stats* stats) {
+  return hest_common(ctx, d_coords, n_rows, n_cols, cols, n_sel, mode, h_init, skip_levels,
+                     h_out, stats, true);
+}
+
+}  // extern "C"

@@ -15,11 +15,12 @@ from typing import Sequence
 import numpy as np
 
 from . import _native
-from ._native import CallStats, Instance, c_f32_p, c_f64_p, c_size_p, c_u32_p
+from ._native import CallStats, HestStats, Instance, c_f32_p, c_f64_p, c_size_p, c_u32_p
 
 COMPAT_NORM = 1
 BATCH_SUPPORT_COUNTS = 2
 BATCH_DEVICE_INPUT = 4
+HEST_THUMB, HEST_AMISE, HEST_AMISE_WARM = 0, 1, 2
 
 
 def as_colmajor(coords, n_rows: int | None = None) -> tuple[np.ndarray, int, int]:
@@ -212,6 +213,48 @@ class Context:
                                          flags, out.ctypes.data_as(c_f64_p))
         self.check(st)
         return out
+
+
+    # ------------------------------------------------- bandwidth estimation
+    def epa_convolution(self, sorted_coords, h: float) -> float:
+        """1/n^2 sum_ij max(0, 4.5 - 2.25 |x_i - x_j| / h) (reference
+        epa_convolution, densities_omp.cpp:235-277)."""
+        x = np.ascontiguousarray(np.asarray(sorted_coords, dtype=np.float32).ravel())
+        out = C.c_float(0.0)
+        self.check(self._lib.ent_epa_convolution(self._h, x.ctypes.data_as(C.c_void_p), x.size,
+                                                 float(h), C.byref(out)))
+        return float(out.value)
+
+    def hestimate(self, coords, mode: int = HEST_AMISE, cols: Sequence[int] | None = None,
+                  h_init: Sequence[float] | None = None, skip_levels: int = 0
+                  ) -> tuple[np.ndarray, list[dict]]:
+        """Per-column bandwidths (Thumb or AMISE search; warm-started from
+        h_init when mode == HEST_AMISE_WARM). coords: (n_cols, n_rows)."""
+        flat, n_rows, n_cols = as_colmajor(coords)
+        sel = np.arange(n_cols, dtype=np.uint32) if cols is None else _u32(cols)
+        hout = np.zeros(len(sel), dtype=np.float32)
+        hin = None if h_init is None else _f32(h_init)
+        st = (HestStats * len(sel))()
+        self.check(self._lib.ent_hestimate(
+            self._h, flat.ctypes.data_as(C.c_void_p), n_rows, n_cols, sel.ctypes.data_as(c_u32_p),
+            len(sel), int(mode), hin.ctypes.data_as(c_f32_p) if hin is not None else None,
+            int(skip_levels), hout.ctypes.data_as(c_f32_p), C.cast(st, C.c_void_p)))
+        return hout, [dict(h0=s.h0, conv_evals=s.conv_evals, levels_skipped=s.levels_skipped,
+                           warm_converged=s.warm_converged) for s in st]
+
+    def hestimate_device(self, d_coords: int, n_rows: int, n_cols: int, mode: int = HEST_AMISE,
+                         h_init: Sequence[float] | None = None, skip_levels: int = 0
+                         ) -> tuple[np.ndarray, list[dict]]:
+        sel = np.arange(n_cols, dtype=np.uint32)
+        hout = np.zeros(n_cols, dtype=np.float32)
+        hin = None if h_init is None else _f32(h_init)
+        st = (HestStats * n_cols)()
+        self.check(self._lib.ent_hestimate_device(
+            self._h, C.c_void_p(d_coords), n_rows, n_cols, sel.ctypes.data_as(c_u32_p), n_cols,
+            int(mode), hin.ctypes.data_as(c_f32_p) if hin is not None else None,
+            int(skip_levels), hout.ctypes.data_as(c_f32_p), C.cast(st, C.c_void_p)))
+        return hout, [dict(h0=s.h0, conv_evals=s.conv_evals, levels_skipped=s.levels_skipped,
+                           warm_converged=s.warm_converged) for s in st]
 
 
 _default: Context | None = None

@@ -149,6 +149,52 @@ typedef struct {
 int ent_entropy_batch(ent_ctx* ctx, const ent_instance* inst, size_t n_inst,
                       uint32_t flags, double* h_out);
 
+/* ---------------------------------------------- bandwidth estimation */
+
+/*
+ * Convolution of the Epanechnikov kernel with itself over all pairs,
+ *   out = 1/n^2 sum_i sum_j max(0, 4.5 - 2.25 |x_i - x_j| / h),
+ * the AMISE helper of the reference. Replaces
+ *   float epa_convolution(const std::vector<float>& sorted_coords, float h)
+ * (densities_cuda.hpp:26-31; OpenMP form densities_omp.cpp:235-277).
+ * Input need not be sorted. Host memory.
+ */
+int ent_epa_convolution(ent_ctx* ctx, const float* sorted_coords, size_t n,
+                        float h, float* out);
+
+/* modes of ent_hestimate */
+#define ENT_HEST_THUMB 0u      /* h0 = n^(-1/7) sqrt(var) (hestimate.cpp:19-30) */
+#define ENT_HEST_AMISE 1u      /* AMISE interval search (hestimate.cpp:41-104) */
+#define ENT_HEST_AMISE_WARM 2u /* the same search entered skip_levels levels
+                                  deep, at the bracket node containing h_init,
+                                  with a full search for columns whose warm
+                                  search ends against an inner node edge */
+
+typedef struct {
+  float h0;                /* rule-of-thumb start value */
+  uint32_t conv_evals;     /* convolution evaluations spent */
+  uint32_t levels_skipped; /* warm start: levels taken from h_init */
+  uint32_t warm_converged; /* warm start: 1 if no full search was needed */
+} ent_hest_stats;
+
+/*
+ * Per-column bandwidths of the selected columns cols[0..n_sel) (all columns
+ * if cols is NULL), every column searched at once on the device. Replaces
+ * Hestimate::main<KRNL> (hestimate.hxx:6-26) with Thumb::Kernel or
+ * AmiseMin::Kernel. h_init (warm mode): one start value per selected column.
+ * stats (nullable): one entry per selected column. Host memory.
+ */
+int ent_hestimate(ent_ctx* ctx, const float* coords, size_t n_rows,
+                  size_t n_cols, const uint32_t* cols, size_t n_sel,
+                  uint32_t mode, const float* h_init, uint32_t skip_levels,
+                  float* h_out, ent_hest_stats* stats);
+/* Same with coords in device memory (h_init, h_out, stats on the host). */
+int ent_hestimate_device(ent_ctx* ctx, const float* d_coords, size_t n_rows,
+                         size_t n_cols, const uint32_t* cols, size_t n_sel,
+                         uint32_t mode, const float* h_init,
+                         uint32_t skip_levels, float* h_out,
+                         ent_hest_stats* stats);
+
 #ifdef __cplusplus
 }
 #endif

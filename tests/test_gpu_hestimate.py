@@ -1,0 +1,59 @@
+"""GPU parity of the AMISE convolution and the on-device bandwidth search
+against the reference (golden fixtures) and the FP64 oracle."""
+import numpy as np
+import pytest
+
+from entropical_gb300 import workloads
+from entropical_gb300.densities import HEST_AMISE, HEST_AMISE_WARM, HEST_THUMB
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def test_convolution_golden(ctx, golden):
+    for h, v in zip(golden["conv_h"], golden["conv_v"]):
+        c = ctx.epa_convolution(golden["conv_x"], float(h))
+        assert abs(c - v) / v < 2e-6
+
+
+@pytest.mark.parametrize("n", [1, 7, 5000, 60000])
+def test_convolution_fp64(ctx, n):
+    x = np.sort(workloads.gmm_1d(n, seed=n))
+    for h in (0.01, 0.2, 3.0):
+        assert abs(ctx.epa_convolution(x, h) - O.epa_conv_fp64(x, h)) / O.epa_conv_fp64(x, h) < 2e-6
+
+
+def test_convolution_unsorted_input(ctx):
+    x = workloads.gmm_1d(3000, seed=4)
+    assert abs(ctx.epa_convolution(x, 0.1) - O.epa_conv_fp64(np.sort(x), 0.1)) < 1e-6
+
+
+def test_hestimate_golden(ctx, golden):
+    h, st = ctx.hestimate(golden["hest_x"], HEST_AMISE)
+    assert np.array_equal(h, golden["hest_amise"])
+    assert all(s["conv_evals"] == 16 for s in st)
+    t, _ = ctx.hestimate(golden["hest_x"], HEST_THUMB)
+    assert np.array_equal(t, golden["hest_thumb"])
+
+
+def test_hestimate_matches_restatement(ctx):
+    rng = np.random.default_rng(12)
+    cols = np.stack([workloads.mixture_instance(rng, 1, 5000)[0] for _ in range(6)])
+    h, _ = ctx.hestimate(cols, HEST_AMISE)
+    for c, hc in zip(cols, h):
+        assert O.hestimate_amise(c, exact=False)[0] == hc
+        assert O.thumb_ref(c) * (2 - 1.9 / 512) == pytest.approx(hc, rel=1e-6)
+
+
+def test_warm_start_saves_levels_and_is_exact(ctx):
+    rng = np.random.default_rng(13)
+    cols = np.stack([workloads.mixture_instance(rng, 1, 20000)[0] for _ in range(5)])
+    full, sf = ctx.hestimate(cols, HEST_AMISE)
+    h0 = np.array([s["h0"] for s in sf], np.float32)
+    warm, sw = ctx.hestimate(cols, HEST_AMISE_WARM, h_init=1.99 * h0, skip_levels=6)
+    assert np.array_equal(warm, full)
+    assert all(s["conv_evals"] == 4 and s["warm_converged"] == 1 for s in sw)
+    # a poor start ends against an inner node edge and falls back
+    bad, sb = ctx.hestimate(cols, HEST_AMISE_WARM, h_init=0.3 * h0, skip_levels=6)
+    assert np.array_equal(bad, full)
+    assert all(s["warm_converged"] == 0 and s["conv_evals"] == 20 for s in sb)
