@@ -34,6 +34,11 @@ class CallStats(C.Structure):
     ]
 
 
+class Tuning(C.Structure):
+    """ent_tuning: pair-kernel tile shapes."""
+    _fields_ = [("targets_per_warp", C.c_uint32 * 3), ("cells_per_h", C.c_uint32)]
+
+
 class NativeError(RuntimeError):
     def __init__(self, status: int, msg: str):
         super().__init__(f"entropical_gb300 status {status}: {msg}")
@@ -47,6 +52,8 @@ SIGNATURES: dict[str, tuple] = {
     "ent_status_string": (C.c_char_p, [C.c_int]),
     "ent_last_error": (C.c_char_p, [C.c_void_p]),
     "ent_last_stats": (C.c_int, [C.c_void_p, C.POINTER(CallStats)]),
+    "ent_set_tuning": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "ent_get_tuning": (C.c_int, [C.c_void_p, C.c_void_p]),
     "ent_densities": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, c_u32_p, c_f32_p,
                                 c_u32_p, C.c_uint32, C.c_uint32, C.c_void_p, c_size_p]),
     "ent_densities_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, c_u32_p,
@@ -59,6 +66,12 @@ SIGNATURES: dict[str, tuple] = {
     "ent_mi_all_pairs_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t,
                                           c_f32_p, C.c_uint32, c_f64_p, c_f64_p]),
     "ent_entropy_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_uint32, c_f64_p]),
+    "ent_te_all_pairs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, c_f32_p,
+                                   c_u32_p, C.c_size_t, C.c_uint32, c_f64_p]),
+    "ent_te_all_pairs_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t,
+                                          c_f32_p, c_u32_p, C.c_size_t, C.c_uint32, c_f64_p]),
+    "ent_neighbor_counts": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_float, C.c_uint32,
+                                      C.c_void_p, C.c_void_p, C.POINTER(C.c_uint64)]),
     "ent_epa_convolution": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_float, c_f32_p]),
     "ent_hestimate": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, c_u32_p,
                                 C.c_size_t, C.c_uint32, c_f32_p, C.c_uint32, c_f32_p,

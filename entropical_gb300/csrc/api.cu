@@ -267,13 +267,20 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
       I.n = s.n;
       I.d = s.d;
       max_n = std::max(max_n, s.n);
-      double prod_h = 1.0;
+      double prod_hg2 = 1.0;
       for (uint32_t j = 0; j < s.d; ++j) {
         const ViewStats& st_j = vs[s.view[j]];
         I.x[j] = views[s.view[j]].x;
-        I.center[j] = 0.5f * (st_j.mn + st_j.mx);
-        I.inv_h[j] = 1.0f / s.h[j];
-        prod_h *= (double)s.h[j];
+        // exact power-of-two scale with g = h 2^k in [1, 2), limited so that
+        // no scaled coordinate can overflow
+        int k = -std::ilogb(s.h[j]);
+        const double amax = std::max(std::fabs((double)st_j.mn), std::fabs((double)st_j.mx));
+        while (k > -126 && amax * std::ldexp(1.0, k) > 1e37) --k;
+        k = std::max(-126, std::min(126, k));
+        I.sc[j] = std::ldexp(1.0f, k);
+        const float g = s.h[j] * I.sc[j];
+        I.g2[j] = g * g;
+        prod_hg2 *= (double)s.h[j] * (double)I.g2[j];
       }
       I.perm0 = vvals + voff[s.view[0]];
       I.S = s.d == 2 ? std::max(1u, std::min(4u, s.S)) : 1u;
@@ -299,11 +306,11 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
       }
       I.n_strips = I.ncell1 * I.ncell2;
       max_strips = std::max(max_strips, I.n_strips);
-      I.tt = (uint32_t)density_tile_targets((int)s.d);
+      I.tt = (uint32_t)density_tile_targets((int)s.d, c.tile_r[s.d - 1]);
       I.tile_cap = (s.n + I.tt - 1) / I.tt + std::min(I.n_strips, s.n);
       I.tile_base = slot;
       slot += I.tile_cap;
-      I.scale = (mode & DM_COUNT) ? 1.0 : std::pow(0.75, (double)s.d) / (s.norm * prod_h);
+      I.scale = (mode & DM_COUNT) ? 1.0 : std::pow(0.75, (double)s.d) / (s.norm * prod_hg2);
       I.out = s.out;
     }
     group_slots[d] = slot - group_base[d];
@@ -412,7 +419,7 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
     if (group_slots[d] == 0) continue;
     int launched = 0;
     cudaEventRecord(c.ev_d[d - 1][0], st);
-    e = launch_density(st, d, tiles + group_base[d], group_slots[d], di_sorted,
+    e = launch_density(st, d, c.tile_r[d - 1], tiles + group_base[d], group_slots[d], di_sorted,
                        wc + d, c.d_err, tile_ls + group_base[d], mode, c.n_sms,
                        &launched);
     if (e != cudaSuccess) return c.cuda_fail(e, "density kernel");
@@ -542,6 +549,27 @@ const char* ent_status_string(int s) {
     case ENT_ERR_STATE: return "invalid state";
   }
   return "unknown status";
+}
+
+int ent_set_tuning(ent_ctx* ctx, const ent_tuning* t) {
+  if (!ctx || !t) return ENT_ERR_ARG;
+  Ctx* c = reinterpret_cast<Ctx*>(ctx);
+  for (int d = 1; d <= 3; ++d)
+    if (t->targets_per_warp[d - 1] && !density_r_supported(d, (int)t->targets_per_warp[d - 1]))
+      return c->fail(ENT_ERR_ARG, "unsupported targets_per_warp");
+  if (t->cells_per_h > 4) return c->fail(ENT_ERR_ARG, "cells_per_h must be 1..4");
+  for (int d = 1; d <= 3; ++d)
+    if (t->targets_per_warp[d - 1]) c->tile_r[d - 1] = (int)t->targets_per_warp[d - 1];
+  if (t->cells_per_h) c->strip_subdiv = t->cells_per_h;
+  return ENT_OK;
+}
+
+int ent_get_tuning(const ent_ctx* ctx, ent_tuning* t) {
+  if (!ctx || !t) return ENT_ERR_ARG;
+  const Ctx* c = reinterpret_cast<const Ctx*>(ctx);
+  for (int d = 0; d < 3; ++d) t->targets_per_warp[d] = (uint32_t)c->tile_r[d];
+  t->cells_per_h = c->strip_subdiv;
+  return ENT_OK;
 }
 
 const char* ent_last_error(const ent_ctx* ctx) {

@@ -39,6 +39,7 @@ struct Ctx {
   ent_call_stats stats{};
   bool pending_pairs = false;
   uint32_t strip_subdiv = 2;  // cells per bandwidth along dimension 1 (d = 2)
+  int tile_r[3] = {16, 16, 8};  // targets per warp of the pair kernel, by d
 
   // grid of a persistent kernel: resident CTAs per SM x SMs, capped by work
   unsigned persistent_grid(uint32_t n_work, const void* kern, int threads, size_t smem);

@@ -124,9 +124,113 @@ int mi_impl(ent_ctx* ctx, const float* coords, size_t n_rows, size_t n_cols,
   return ENT_OK;
 }
 
+// TE_{j->i}(tau) = H(y_i, x_j) + H(y_i^+, y_i) - H(y_i^+, y_i, x_j) - H(y_i)
+// over the n = N - tau samples t (y_i = x_i[t], y_i^+ = x_i[t + tau],
+// x_j = x_j[t]); one batch over every lag and ordered pair.
+int te_impl(ent_ctx* ctx, const float* coords, size_t n_rows, size_t n_cols, const float* h,
+            const uint32_t* taus, size_t n_taus, uint32_t flags, double* te_out,
+            bool device_in) {
+  if (!ctx) return ENT_ERR_ARG;
+  Ctx& c = *reinterpret_cast<Ctx*>(ctx);
+  int s = c.begin_call();
+  if (s) return s;
+  if (!coords || !h || !taus || !te_out || n_taus == 0)
+    return c.fail(ENT_ERR_ARG, "null argument");
+  if (n_cols < 1) return c.fail(ENT_ERR_ARG, "empty input");
+  if (n_rows > 0xffffff00ull) return c.fail(ENT_ERR_TOO_LARGE, "too many rows");
+  for (size_t q = 0; q < n_taus; ++q)
+    if (taus[q] == 0 || taus[q] >= n_rows) return c.fail(ENT_ERR_ARG, "lag out of range");
+  for (size_t j = 0; j < n_cols; ++j)
+    if (!(h[j] > 0.f) || !std::isfinite(h[j]))
+      return c.fail(ENT_ERR_ARG, "bandwidth must be finite and positive");
+  const float* dc = coords;
+  if (!device_in) {
+    float* p = static_cast<float*>(c.arena.alloc(4 * n_rows * n_cols));
+    if (!p) return c.fail(ENT_ERR_CUDA, "out of device memory");
+    cudaError_t e = cudaMemcpyAsync(p, coords, 4 * n_rows * n_cols, cudaMemcpyHostToDevice,
+                                    c.stream);
+    if (e != cudaSuccess) return c.cuda_fail(e, "copy coordinates");
+    dc = p;
+  }
+  const size_t M = n_cols;
+  std::vector<ViewSpec> views;
+  std::vector<InstSpec> insts;
+  // index helpers: per lag, [M 1-D][M 2-D lag][M(M-1)/2 2-D joint][M(M-1) 3-D]
+  const size_t per_tau = M + M + M * (M - 1) / 2 + M * (M - 1);
+  insts.reserve(per_tau * n_taus);
+  for (size_t q = 0; q < n_taus; ++q) {
+    const uint32_t tau = taus[q];
+    const uint32_t n = (uint32_t)(n_rows - tau);
+    const uint32_t v0 = (uint32_t)views.size();
+    for (size_t j = 0; j < M; ++j) views.push_back({dc + j * n_rows, n});        // x_j[t]
+    for (size_t j = 0; j < M; ++j) views.push_back({dc + j * n_rows + tau, n});  // x_j[t+tau]
+    auto mk = [&](uint32_t d, uint32_t a, uint32_t b, uint32_t cc, float ha, float hb,
+                  float hc) {
+      InstSpec I;
+      I.d = d;
+      I.n = n;
+      I.view[0] = a;
+      I.view[1] = b;
+      I.view[2] = cc;
+      I.h[0] = ha;
+      I.h[1] = hb;
+      I.h[2] = hc;
+      I.norm = (double)n;
+      I.S = c.strip_subdiv;
+      insts.push_back(I);
+    };
+    for (size_t i = 0; i < M; ++i) mk(1, v0 + i, 0, 0, h[i], 1.f, 1.f);
+    for (size_t i = 0; i < M; ++i) mk(2, v0 + M + i, v0 + i, 0, h[i], h[i], 1.f);
+    for (size_t i = 0; i < M; ++i)
+      for (size_t j = i + 1; j < M; ++j) mk(2, v0 + i, v0 + j, 0, h[i], h[j], 1.f);
+    for (size_t i = 0; i < M; ++i)
+      for (size_t j = 0; j < M; ++j)
+        if (i != j) mk(3, v0 + M + i, v0 + i, v0 + j, h[i], h[i], h[j]);
+  }
+  std::vector<double> H;
+  const bool counts = (flags & ENT_BATCH_SUPPORT_COUNTS) != 0;
+  s = run_entropies(c, views, insts, counts, &H);
+  if (s) return s;
+  s = c.end_call();
+  c.collect_kernel_stats();
+  if (s) return s;
+  std::vector<size_t> pair_idx(M * M, 0);
+  for (size_t i = 0, k = 0; i < M; ++i)
+    for (size_t j = i + 1; j < M; ++j, ++k) pair_idx[i * M + j] = pair_idx[j * M + i] = k;
+  for (size_t q = 0; q < n_taus; ++q) {
+    const size_t b = q * per_tau;
+    const size_t b2l = b + M, b2j = b + 2 * M, b3 = b + 2 * M + M * (M - 1) / 2;
+    double* T = te_out + q * M * M;
+    size_t k3 = 0;
+    for (size_t i = 0; i < M; ++i)
+      for (size_t j = 0; j < M; ++j) {
+        if (i == j) {
+          T[i * M + j] = counts ? H[b + i] : 0.0;
+          continue;
+        }
+        const double h3 = H[b3 + k3++];
+        T[i * M + j] = counts ? h3 : H[b2j + pair_idx[i * M + j]] + H[b2l + i] - h3 - H[b + i];
+      }
+  }
+  return ENT_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+int ent_te_all_pairs(ent_ctx* ctx, const float* coords, size_t n_rows, size_t n_cols,
+                     const float* h, const uint32_t* taus, size_t n_taus, uint32_t flags,
+                     double* te_out) {
+  return te_impl(ctx, coords, n_rows, n_cols, h, taus, n_taus, flags, te_out, false);
+}
+
+int ent_te_all_pairs_device(ent_ctx* ctx, const float* d_coords, size_t n_rows,
+                            size_t n_cols, const float* h, const uint32_t* taus,
+                            size_t n_taus, uint32_t flags, double* te_out) {
+  return te_impl(ctx, d_coords, n_rows, n_cols, h, taus, n_taus, flags, te_out, true);
+}
+
 
 int ent_mi_all_pairs(ent_ctx* ctx, const float* coords, size_t n_rows,
                      size_t n_cols, const float* h, uint32_t flags,

@@ -31,7 +31,7 @@ using namespace ent;
 namespace {
 
 struct ConvCol {
-  const float* xs;  // sorted, centred column (n + 8 floats)
+  const float* xs;  // value-sorted column (n + 8 floats)
   uint32_t n;
   uint32_t tile_base;
   uint32_t n_tiles;
@@ -85,7 +85,7 @@ __global__ void k_gather_sorted(const ConvCol* __restrict__ cols,
   float* xs = const_cast<float*>(C.xs);
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < C.n + 8;
        k += gridDim.x * blockDim.x)
-    xs[k] = k < C.n ? __fsub_rn(x[p[k]], center[blockIdx.y]) : 0.f;
+    xs[k] = k < C.n ? x[p[k]] : 0.f;
 }
 
 __device__ __forceinline__ float piv_of(double a, double b) { return (float)(a + b); }

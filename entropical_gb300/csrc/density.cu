@@ -4,16 +4,19 @@
 // density_{1,2,3}d_krnl (density_1d.cuh:51-90, density_2d.cuh:57-100,
 // density_3d.cuh:61-108) and the OpenMP window loops
 // (densities_omp.cpp:33-159). For every target point t
-//     S_t = sum_s prod_j max(0, 1 - (y_tj - y_sj)^2),   y = (x - c)/h,
-//     p_t = 0.75^d / (norm * prod_j h_j) * S_t,
-// which equals the reference's sum of 0.75 (1-u^2)/h products.
+//     S_t = sum_s prod_j max(0, g_j^2 - (y_tj - y_sj)^2),   y_j = x_j 2^k_j,
+//     p_t = 0.75^d / (norm * prod_j h_j g_j^2) * S_t,
+// with 2^k_j an exact power of two such that g_j = h_j 2^k_j lies in [1, 2).
+// Since (y_t - y_s)/g = (x_t - x_s)/h exactly, this equals the reference's
+// sum of 0.75 (1-u^2)/h products, and the coordinate differences carry the
+// precision of the raw float data, as in the reference's (ref - val)/h.
 //
 // Cell lists ("strips"): points are sorted on dimension 0; dimensions 1..d-1
 // are binned into cells of width h/S, and a stable partition by cell keeps
 // dimension-0 order inside each strip. A target tile (up to TT consecutive
 // points of one strip) then sees all of its in-support sources inside
 // (2S+1)^(d-1) contiguous runs: one per neighbouring strip, clipped by
-// binary search to [y0_first - 1, y0_last + 1]. This is the device form of
+// binary search to [y0_first - g0, y0_last + g0]. This is the device form of
 // the reference's sorted-window search boxes() (densities_omp.cpp:33-65) and
 // of the cell boxes of Transs::BoxedSearch (boxedsearch.cpp:15-62).
 //
@@ -202,16 +205,15 @@ __global__ void k_gather_pts(const InstDev* __restrict__ insts) {
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < I.n;
        k += gridDim.x * blockDim.x) {
     const uint32_t j = I.perm[k];
-    const float y0 = __fmul_rn(__fsub_rn(I.x[0][j], I.center[0]), I.inv_h[0]);
+    // multiplication by a power of two is exact
+    const float y0 = I.x[0][j] * I.sc[0];
     if (I.d == 1) {
       reinterpret_cast<float*>(I.pts)[k] = y0;
     } else if (I.d == 2) {
-      const float y1 = __fmul_rn(__fsub_rn(I.x[1][j], I.center[1]), I.inv_h[1]);
-      reinterpret_cast<float2*>(I.pts)[k] = make_float2(y0, y1);
+      reinterpret_cast<float2*>(I.pts)[k] = make_float2(y0, I.x[1][j] * I.sc[1]);
     } else {
-      const float y1 = __fmul_rn(__fsub_rn(I.x[1][j], I.center[1]), I.inv_h[1]);
-      const float y2 = __fmul_rn(__fsub_rn(I.x[2][j], I.center[2]), I.inv_h[2]);
-      reinterpret_cast<float4*>(I.pts)[k] = make_float4(y0, y1, y2, 0.f);
+      reinterpret_cast<float4*>(I.pts)[k] =
+          make_float4(y0, I.x[1][j] * I.sc[1], I.x[2][j] * I.sc[2], 0.f);
     }
   }
 }
@@ -274,8 +276,11 @@ __global__ void k_plan(const InstDev* __restrict__ insts, uint32_t n_inst,
   const uint32_t tc = min(I.tt, I.strip_start[s + 1] - tb);
   const float yf = y0_at(I.pts, d, tb);
   const float yl = y0_at(I.pts, d, tb + tc - 1);
-  const float eps = 1e-5f * (1.f + fmaxf(fabsf(yf), fabsf(yl)));
-  const float vlo = yf - 1.f - eps, vhi = yl + 1.f + eps;
+  // half-width g0 = sqrt(g0^2), widened so that rounding can only add
+  // candidates (an out-of-support candidate contributes exactly 0)
+  const float g0 = sqrtf(I.g2[0]);
+  const float eps = 1e-5f * (g0 + fmaxf(fabsf(yf), fabsf(yl)));
+  const float vlo = yf - g0 - eps, vhi = yl + g0 + eps;
   td.t_begin = tb;
   td.t_count = tc;
   uint32_t nr = 0;
@@ -337,7 +342,6 @@ __global__ void __launch_bounds__(128)
     fence_mbar_init();
   }
   __syncthreads();
-  const f32x2 M1 = pk2(-1.f, -1.f);
   uint32_t q = 0;
 
   for (;;) {
@@ -370,6 +374,9 @@ __global__ void __launch_bounds__(128)
     const InstDev* I = insts + s_inst;
     const P* __restrict__ pts = reinterpret_cast<const P*>(I->pts);
     const uint32_t nr = s_nr, nsrc = run_pre[nr], tb = s_tb;
+    // -g^2 per dimension: v = d^2 - g^2 <= 0 inside the support
+    const float ng0 = -I->g2[0], ng1 = -I->g2[D > 1 ? 1 : 0], ng2 = -I->g2[D > 2 ? 2 : 0];
+    const f32x2 M1 = (D == 1) ? pk2(ng0, ng0) : pk2(ng0, ng1);
     const uint32_t nch = (nsrc + C::CH - 1) / C::CH;
     if (tid == 0 && nch > 0)
       issue_chunk<D, R>(0, q & 1u, nsrc, nr, run_lo, run_pre, pts, bufs, ptab,
@@ -382,7 +389,7 @@ __global__ void __launch_bounds__(128)
       ks[r] = 0.f;
       kc[r] = 0.f;
     }
-    constexpr float FAR = 1e18f;
+    const float FAR = __int_as_float(0x7f800000);  // +inf: every term is 0
     f32x2 T01[R];
     float T2[R];
 #pragma unroll
@@ -432,15 +439,15 @@ __global__ void __launch_bounds__(128)
                 bool in;
                 if constexpr (D == 1) {
                   const float dd = __fsub_rn(T2[r], s);
-                  in = fmaf(dd, dd, -1.f) <= 0.f;
+                  in = fmaf(dd, dd, ng0) <= 0.f;
                 } else {
                   float tx, ty;
                   upk2(T01[r], tx, ty);
                   const float dx = __fsub_rn(tx, s.x), dy = __fsub_rn(ty, s.y);
-                  in = fmaf(dx, dx, -1.f) <= 0.f && fmaf(dy, dy, -1.f) <= 0.f;
+                  in = fmaf(dx, dx, ng0) <= 0.f && fmaf(dy, dy, ng1) <= 0.f;
                   if constexpr (D == 3) {
                     const float dz = __fsub_rn(T2[r], s.z);
-                    in = in && fmaf(dz, dz, -1.f) <= 0.f;
+                    in = in && fmaf(dz, dz, ng2) <= 0.f;
                   }
                 }
                 acc[r] += in ? 1.f : 0.f;
@@ -508,7 +515,7 @@ __global__ void __launch_bounds__(128)
                 const f32x2 dd = sub2(T01[r], S);
                 const float dz = T2[r] - s.z;
                 const f32x2 v = fma2(dd, dd, M1);
-                const float vz = fmaf(dz, dz, -1.f);
+                const float vz = fmaf(dz, dz, ng2);
                 float vx, vy;
                 upk2(v, vx, vy);
                 const float pxy = fminf(vx, 0.f) * fminf(vy, 0.f);
@@ -619,12 +626,14 @@ __global__ void __launch_bounds__(256)
 
 }  // namespace
 
-// Targets per warp for each dimension (tile = 4 warps).
-constexpr int R1 = 16, R2 = 16, R3 = 8;
-
-int density_tile_targets(int d) {
-  return d == 1 ? Cfg<1, R1>::TT : (d == 2 ? Cfg<2, R2>::TT : Cfg<3, R3>::TT);
+// Targets per warp: the tunable variants of each dimension (tile = 4 warps).
+int density_r_supported(int d, int r) {
+  if (d == 1 || d == 2) return r == 8 || r == 16;
+  if (d == 3) return r == 4 || r == 8;
+  return 0;
 }
+
+int density_tile_targets(int d, int r) { return 4 * r; }
 
 cudaError_t launch_colstats(cudaStream_t st, const ViewDev* views,
                             uint32_t n_views, ViewStats* stats) {
@@ -689,22 +698,22 @@ cudaError_t launch_plan(cudaStream_t st, const InstDev* insts, uint32_t n_inst,
   return cudaGetLastError();
 }
 
-cudaError_t launch_density(cudaStream_t st, int d, const TileDesc* tiles,
+cudaError_t launch_density(cudaStream_t st, int d, int r, const TileDesc* tiles,
                            uint32_t n_slots, const InstDev* insts,
                            uint32_t* work_counter, uint32_t* err,
                            double* tile_logsum, uint32_t mode, int n_sms,
                            int* launched) {
-  switch (d) {
-    case 1:
-      return launch_density_t<1, R1>(st, tiles, n_slots, insts, work_counter,
-                                     err, tile_logsum, mode, n_sms, launched);
-    case 2:
-      return launch_density_t<2, R2>(st, tiles, n_slots, insts, work_counter,
-                                     err, tile_logsum, mode, n_sms, launched);
-    case 3:
-      return launch_density_t<3, R3>(st, tiles, n_slots, insts, work_counter,
-                                     err, tile_logsum, mode, n_sms, launched);
-  }
+#define ENT_LAUNCH(D, R)                                                            \
+  if (d == D && r == R)                                                             \
+    return launch_density_t<D, R>(st, tiles, n_slots, insts, work_counter, err,     \
+                                  tile_logsum, mode, n_sms, launched);
+  ENT_LAUNCH(1, 8)
+  ENT_LAUNCH(1, 16)
+  ENT_LAUNCH(2, 8)
+  ENT_LAUNCH(2, 16)
+  ENT_LAUNCH(3, 4)
+  ENT_LAUNCH(3, 8)
+#undef ENT_LAUNCH
   return cudaErrorInvalidValue;
 }
 

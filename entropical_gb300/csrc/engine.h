@@ -52,15 +52,15 @@ struct InstDev {
   uint32_t tile_base, tile_cap;
   float lo1, lo2;           // cell-grid origins
   double inv_w1, inv_w2;    // inverse cell widths (cell width = h/S, widened)
-  float center[3];
-  float inv_h[3];
+  float sc[3];  // exact power-of-two scale 2^k_j with g_j = h_j 2^k_j in [1, 2)
+  float g2[3];  // g_j^2: the support radius squared in scaled units
   const uint32_t* perm0;    // dimension-0 sorted order (view sort)
   uint32_t* perm;           // final strip-major order
   const uint32_t* skeys;    // sorted strip keys (d >= 2)
-  void* pts;                // sorted, centred, 1/h-scaled points (float/float2/float4)
+  void* pts;                // sorted points x_j * sc_j (float/float2/float4)
   uint32_t* strip_start;    // n_strips + 1
   uint32_t* tile_off;       // n_strips + 1
-  double scale;             // 0.75^d / (norm * prod h)
+  double scale;             // 0.75^d / (norm * prod h_j * prod g_j^2)
   double* out;              // per-point density by original index (nullable)
   uint32_t tt;              // targets per tile
   uint32_t pad;
@@ -102,12 +102,14 @@ cudaError_t launch_gather_pts(cudaStream_t st, const InstDev* insts,
 cudaError_t launch_plan(cudaStream_t st, const InstDev* insts, uint32_t n_inst,
                         const uint32_t* inst_tile_base, TileDesc* tiles,
                         uint32_t n_slots, uint64_t* n_src_total);
-cudaError_t launch_density(cudaStream_t st, int d, const TileDesc* tiles,
+cudaError_t launch_density(cudaStream_t st, int d, int r, const TileDesc* tiles,
                            uint32_t n_slots, const InstDev* insts,
                            uint32_t* work_counter, uint32_t* err,
                            double* tile_logsum, uint32_t mode, int n_sms,
                            int* launched_ctas);
-int density_tile_targets(int d);
+// targets per warp R available for dimension d; tile = 4 warps x R targets
+int density_r_supported(int d, int r);
+int density_tile_targets(int d, int r);
 cudaError_t launch_inst_logsum(cudaStream_t st, const InstDev* insts,
                                uint32_t n_inst, const double* tile_logsum,
                                double* inst_logsum);

@@ -95,6 +95,18 @@ class Context:
         self.check(self._lib.ent_last_stats(self._h, C.byref(s)))
         return s
 
+    def tuning(self) -> dict:
+        t = _native.Tuning()
+        self.check(self._lib.ent_get_tuning(self._h, C.byref(t)))
+        return {"targets_per_warp": list(t.targets_per_warp), "cells_per_h": t.cells_per_h}
+
+    def set_tuning(self, targets_per_warp=(0, 0, 0), cells_per_h: int = 0) -> None:
+        t = _native.Tuning()
+        for i, v in enumerate(targets_per_warp):
+            t.targets_per_warp[i] = int(v)
+        t.cells_per_h = int(cells_per_h)
+        self.check(self._lib.ent_set_tuning(self._h, C.byref(t)))
+
     def _selection(self, i_cols, h, tau):
         d = len(i_cols)
         cols = _u32(i_cols)
@@ -187,6 +199,29 @@ class Context:
         self.check(st)
         return mi, hx
 
+    def te_all_pairs(self, coords, h: Sequence[float], taus: Sequence[int],
+                     counts: bool = False) -> np.ndarray:
+        """All-ordered-pairs transfer entropy; returns (n_taus, M, M) with
+        [q, i, j] = TE_{j->i}(taus[q])."""
+        flat, n_rows, n_cols = as_colmajor(coords)
+        hv, tv = _f32(h), _u32(taus)
+        out = np.zeros((len(tv), n_cols, n_cols), dtype=np.float64)
+        self.check(self._lib.ent_te_all_pairs(
+            self._h, flat.ctypes.data_as(C.c_void_p), n_rows, n_cols, hv.ctypes.data_as(c_f32_p),
+            tv.ctypes.data_as(c_u32_p), len(tv), BATCH_SUPPORT_COUNTS if counts else 0,
+            out.ctypes.data_as(c_f64_p)))
+        return out
+
+    def te_all_pairs_device(self, d_coords: int, n_rows: int, n_cols: int, h, taus,
+                            counts: bool = False) -> np.ndarray:
+        hv, tv = _f32(h), _u32(taus)
+        out = np.zeros((len(tv), n_cols, n_cols), dtype=np.float64)
+        self.check(self._lib.ent_te_all_pairs_device(
+            self._h, C.c_void_p(d_coords), n_rows, n_cols, hv.ctypes.data_as(c_f32_p),
+            tv.ctypes.data_as(c_u32_p), len(tv), BATCH_SUPPORT_COUNTS if counts else 0,
+            out.ctypes.data_as(c_f64_p)))
+        return out
+
     def entropy_batch(self, instances, counts: bool = False, device: bool = False) -> np.ndarray:
         """Resubstitution entropies of [(coords (d, n), h (d,))...] in one batch.
         With device=True, coords entries are raw device addresses and the
@@ -214,6 +249,26 @@ class Context:
         self.check(st)
         return out
 
+
+    # ---------------------------------------------------- neighbour search
+    def neighbor_windows(self, col, h: float) -> tuple[np.ndarray, np.ndarray]:
+        """The reference boxes() source window [lo, hi] of every point."""
+        return self._neighbors(col, h, 0)[:2]
+
+    def boxed_neighbors(self, col, box: float) -> tuple[int, np.ndarray, np.ndarray]:
+        """BoxedSearch: (number of boxes, box of every point, neighbour-list sizes)."""
+        a, b, nb = self._neighbors(col, box, 1)
+        return nb, a, b
+
+    def _neighbors(self, col, h, mode):
+        x = np.ascontiguousarray(np.asarray(col, dtype=np.float32).ravel())
+        a = np.zeros(x.size, np.uint64)
+        b = np.zeros(x.size, np.uint64)
+        nb = C.c_uint64(0)
+        self.check(self._lib.ent_neighbor_counts(self._h, x.ctypes.data_as(C.c_void_p), x.size,
+                                                 float(h), mode, a.ctypes.data_as(C.c_void_p),
+                                                 b.ctypes.data_as(C.c_void_p), C.byref(nb)))
+        return a, b, int(nb.value)
 
     # ------------------------------------------------- bandwidth estimation
     def epa_convolution(self, sorted_coords, h: float) -> float:

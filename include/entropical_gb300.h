@@ -60,6 +60,13 @@ typedef struct {
   float pair_kernel_ms_by_dim[3];     /* device time of each persistent launch */
 } ent_call_stats;
 
+/* Tile shapes of the pair kernel (0 = keep the current value). */
+typedef struct {
+  uint32_t targets_per_warp[3]; /* per density dimension: d=1,2: 8 or 16;
+                                   d=3: 4 or 8 (tile = 4 warps) */
+  uint32_t cells_per_h;         /* d=2 strips: cells per bandwidth, 1..4 */
+} ent_tuning;
+
 /* Context lifecycle. device < 0 selects the current device. */
 int ent_create(ent_ctx** ctx, int device);
 void ent_destroy(ent_ctx* ctx);
@@ -67,6 +74,8 @@ const char* ent_status_string(int status);
 /* Message of the last failing call on ctx (empty if none). */
 const char* ent_last_error(const ent_ctx* ctx);
 int ent_last_stats(const ent_ctx* ctx, ent_call_stats* stats);
+int ent_set_tuning(ent_ctx* ctx, const ent_tuning* tuning);
+int ent_get_tuning(const ent_ctx* ctx, ent_tuning* tuning);
 
 /*
  * Combined product-Epanechnikov densities of d = 1..3 selected, lagged
@@ -132,6 +141,28 @@ int ent_mi_all_pairs_device(ent_ctx* ctx, const float* d_coords, size_t n_rows,
                             size_t n_cols, const float* h, uint32_t flags,
                             double* mi_out, double* h_out);
 
+/*
+ * All-ordered-pairs transfer entropy at every lag in taus, in ONE batch:
+ *   TE_{j->i}(tau) = mean_t log[ p(y+, y, x) p(y) / (p(y, x) p(y+, y)) ]
+ *                  = H(y,x) + H(y+,y) - H(y+,y,x) - H(y),
+ * y = x_i[t], y+ = x_i[t+tau], x = x_j[t], t < n_rows - tau, bandwidth h[c]
+ * for column c in every density (as transs.cpp:56-74 reuses them).
+ * te_out: n_taus x n_cols x n_cols, te_out[q][i][j] = TE_{j->i}(taus[q]),
+ * the reference's transs[i*n+j] layout (transs.cpp:75-113), zero diagonal.
+ * Replaces the per-pair density loop of Transs::main (transs.cpp:39-115);
+ * its own sum of p * h^3 * log(...) terms is the reference's formula, this
+ * is the resubstitution estimator. With ENT_BATCH_SUPPORT_COUNTS, te_out
+ * receives the in-support pair counts of the 3-D densities (diagonal: of
+ * the 1-D ones). coords: host memory, column-major n_rows x n_cols.
+ */
+int ent_te_all_pairs(ent_ctx* ctx, const float* coords, size_t n_rows,
+                     size_t n_cols, const float* h, const uint32_t* taus,
+                     size_t n_taus, uint32_t flags, double* te_out);
+/* Same with coords in device memory (te_out on the host). */
+int ent_te_all_pairs_device(ent_ctx* ctx, const float* d_coords, size_t n_rows,
+                            size_t n_cols, const float* h, const uint32_t* taus,
+                            size_t n_taus, uint32_t flags, double* te_out);
+
 /* One density instance of an uneven batch. */
 typedef struct {
   const float* coords; /* column-major d x n: dimension j at coords[j*n + i] */
@@ -148,6 +179,27 @@ typedef struct {
  */
 int ent_entropy_batch(ent_ctx* ctx, const ent_instance* inst, size_t n_inst,
                       uint32_t flags, double* h_out);
+
+/* ---------------------------------------------------- neighbour search */
+
+#define ENT_NB_WINDOW 0u /* reference boxes() windows (densities_omp.cpp:33-65) */
+#define ENT_NB_BOXED 1u  /* Transs::BoxedSearch::Boxes (boxedsearch.cpp:15-62) */
+
+/*
+ * Neighbour search of one column of n values (host memory), bit-exact with
+ * the reference's float arithmetic.
+ * ENT_NB_WINDOW, width h: out_a[i] = first, out_b[i] = last index of the
+ *   value-sorted column whose distance to x_i is below h (strict), i.e. the
+ *   source range the reference density loop visits for point i.
+ * ENT_NB_BOXED, box size h: out_a[i] = box of point i, out_b[i] = size of its
+ *   neighbour list (own and adjacent boxes); *n_boxes = number of boxes.
+ *   The reference's undefined cases are defined: the maximum is the true
+ *   maximum, a box index equal to the box count joins the last box, and a
+ *   zero-width range has one box.
+ */
+int ent_neighbor_counts(ent_ctx* ctx, const float* col, size_t n, float h,
+                        uint32_t mode, uint64_t* out_a, uint64_t* out_b,
+                        uint64_t* n_boxes);
 
 /* ---------------------------------------------- bandwidth estimation */
 

@@ -61,3 +61,25 @@ def test_uneven_batch(ctx):
         x, h = insts[q]
         p = ctx.combined_densities(x, None, list(range(x.shape[0])), h)
         assert abs(H[q] + np.mean(np.log(p))) < 1e-9
+
+
+def test_te_all_pairs_matches_oracle(ctx):
+    x, _ = workloads.langevin(n_coords=4, n_steps=4000, seed=2)
+    h = workloads.scott_bandwidth(x, 3)
+    taus = [1, 5]
+    te = ctx.te_all_pairs(x, h, taus)
+    assert te.shape == (2, 4, 4)
+    for q, tau in enumerate(taus):
+        for i, j in [(0, 1), (2, 0), (3, 2)]:
+            ref = O.te_fp64(x[j], x[i], tau, h[j], h[i])
+            assert abs(te[q, i, j] - ref) < 1e-6
+        assert np.all(np.diag(te[q]) == 0)
+
+
+def test_te_support_counts(ctx):
+    x, _ = workloads.langevin(n_coords=3, n_steps=2000, seed=3)
+    h = workloads.scott_bandwidth(x, 3)
+    cnt = ctx.te_all_pairs(x, h, [2], counts=True)
+    # 3-D instance (y+, y, x) for i=1, j=2
+    c = ctx.support_counts(x, None, [1, 1, 2], [h[1], h[1], h[2]], [2, 0, 0])
+    assert cnt[0, 1, 2] == c.sum()

@@ -102,15 +102,17 @@ def test_support_counts_exact(ctx, d):
     h = np.array([0.3, 0.4, 0.5][:d], np.float32)
     cols = [0, 1, 2][:d]
     c = ctx.support_counts(x, None, cols, h)
-    # brute force with the kernel's own float32 test fma(d, d, -1) <= 0 on
-    # centred, 1/h-scaled coordinates is what the GPU counts; away from the
-    # boundary this equals |x_i - x_k| <= h in exact arithmetic
-    y = [(x[c_] - 0.5 * (x[c_].min() + x[c_].max())) * np.float32(1.0 / h[j])
-         for j, c_ in enumerate(cols)]
+    # brute force with the kernel's own test: coordinates scaled by the exact
+    # power of two 2^k (g = h 2^k in [1, 2)), fma(d, d, -g^2) <= 0, which
+    # equals d*d <= g^2 in exact arithmetic
     inside = np.ones((n, n), bool)
-    for yy in y:
-        dd = (yy[:, None] - yy[None, :]).astype(np.float64)
-        inside &= dd * dd <= 1.0
+    for j, c_ in enumerate(cols):
+        k = 1 - np.frexp(np.float32(h[j]))[1]
+        sc = np.float32(2.0 ** k)
+        g = np.float32(h[j]) * sc
+        y = x[c_] * sc
+        dd = (y[:, None] - y[None, :]).astype(np.float64)
+        inside &= dd * dd <= np.float64(np.float32(g * g))
     assert np.array_equal(c, inside.sum(1).astype(np.float64))
 
 
