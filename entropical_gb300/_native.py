@@ -72,6 +72,21 @@ SIGNATURES: dict[str, tuple] = {
                                           c_f32_p, c_u32_p, C.c_size_t, C.c_uint32, c_f64_p]),
     "ent_neighbor_counts": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_float, C.c_uint32,
                                       C.c_void_p, C.c_void_p, C.POINTER(C.c_uint64)]),
+    "ent_hestimate_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_uint32, c_f32_p,
+                                      C.c_void_p]),
+    "ent_hestimate_learned": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,
+                                        C.c_uint32, C.c_uint32, c_f32_p, C.c_void_p]),
+    "ent_mlp_param_count": (C.c_size_t, []),
+    "ent_mlp_create": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]),
+    "ent_mlp_destroy": (None, [C.c_void_p]),
+    "ent_mlp_set_params": (C.c_int, [C.c_void_p, c_f32_p, c_f32_p, c_f32_p]),
+    "ent_mlp_get_params": (C.c_int, [C.c_void_p, c_f32_p, c_f32_p, c_f32_p]),
+    "ent_mlp_forward": (C.c_int, [C.c_void_p, C.c_void_p, c_f32_p, C.c_size_t, c_f32_p]),
+    "ent_mlp_gradients": (C.c_int, [C.c_void_p, C.c_void_p, c_f32_p, c_f32_p, c_f32_p,
+                                    C.c_size_t, c_f32_p, c_f32_p]),
+    "ent_mlp_train_step": (C.c_int, [C.c_void_p, C.c_void_p, c_f32_p, c_f32_p, c_f32_p,
+                                     C.c_size_t, C.c_float, c_f32_p]),
+    "ent_features": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, c_f32_p]),
     "ent_epa_convolution": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_float, c_f32_p]),
     "ent_hestimate": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, c_u32_p,
                                 C.c_size_t, C.c_uint32, c_f32_p, C.c_uint32, c_f32_p,

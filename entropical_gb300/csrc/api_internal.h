@@ -84,7 +84,15 @@ int sort_views(Ctx& c, const std::vector<ViewSpec>& views, SortedViews* out);
 // interval search; 2: search warm-started from the given bandwidths.
 int hestimate_engine(Ctx& c, const float* raw, const std::vector<uint64_t>& raw_off,
                      const std::vector<uint32_t>& lens, int mode, const float* h_fixed_or_init,
-                     int skip, float* h_out, float* conv_out, ent_hest_stats* stats);
+                     int skip, float* h_out, float* conv_out, ent_hest_stats* stats,
+                     const float* d_log_ratio);
+
+// Learned warm start (mlp.cu): features of device instances and the MLP
+// forward pass on device data.
+int mlp_features_device(Ctx& c, const std::vector<const float*>& base,
+                        const std::vector<uint32_t>& n, const std::vector<uint32_t>& d,
+                        float* d_feat);
+int mlp_forward_device(Ctx& c, ent_mlp* net, float* d_feat, size_t B, float* d_out);
 
 struct EngineOut {
   double* d_logsum_sorted = nullptr;  // per instance, in slot order

@@ -94,7 +94,8 @@ __device__ __forceinline__ float piv_of(double a, double b) { return (float)(a +
 // `skip` levels of the same dyadic bracket tree towards h_init without
 // evaluating anything, then search from there.
 __global__ void k_hest_init(HestState* __restrict__ st, uint32_t n_cols,
-                            const float* __restrict__ h_init, int skip, int fixed_h) {
+                            const float* __restrict__ h_init, int skip, int fixed_h,
+                            const float* __restrict__ log_ratio) {
   const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= n_cols) return;
   HestState s = st[c];
@@ -115,9 +116,10 @@ __global__ void k_hest_init(HestState* __restrict__ st, uint32_t n_cols,
   s.hi = 2.f * s.h0;
   s.glo = s.lo;
   s.ghi = s.hi;
-  if (h_init && skip > 0) {
+  if ((h_init || log_ratio) && skip > 0) {
     s.warm = 1;
-    const float t = h_init[c];
+    // start value: given, or h0 * exp(r) from the learned log-ratio
+    const float t = log_ratio ? s.h0 * expf(log_ratio[c]) : h_init[c];
     for (int k = 0; k < skip; ++k) {
       const float delta = s.hi - s.lo;
       const float pivot = (float)((double)s.lo + 0.5 * (double)delta);
@@ -454,6 +456,12 @@ __global__ void k_conv_single_out(const HestState* __restrict__ st, uint32_t n_c
   if (c < n_cols) out[c] = conv_value(col_sum[2 * c], st[c].n);
 }
 
+__global__ void k_pick(const float* __restrict__ y, const uint32_t* __restrict__ map,
+                       float* __restrict__ out, uint32_t n) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = y[map[i]];
+}
+
 template <class T>
 T* upload(Ctx& c, const std::vector<T>& v, cudaError_t* e) {
   T* p = static_cast<T*>(c.arena.alloc(sizeof(T) * std::max<size_t>(v.size(), 1)));
@@ -496,7 +504,8 @@ constexpr int CONV_R1 = 16, CONV_R2 = 8;
 // bandwidths h_fixed (convolution only), 1 = full search, 2 = warm search.
 int hestimate_engine(Ctx& c, const float* raw, const std::vector<uint64_t>& raw_off,
                      const std::vector<uint32_t>& lens, int mode, const float* h_fixed_or_init,
-                     int skip, float* h_out, float* conv_out, ent_hest_stats* stats) {
+                     int skip, float* h_out, float* conv_out, ent_hest_stats* stats,
+                     const float* d_log_ratio) {
   cudaError_t e;
   const cudaStream_t s = c.stream;
   const uint32_t nc = (uint32_t)lens.size();
@@ -551,8 +560,9 @@ int hestimate_engine(Ctx& c, const float* raw, const std::vector<uint64_t>& raw_
   const unsigned gx = std::min<uint32_t>((std::max(sv.max_n, 1u) + 255) / 256 + 1, 1024);
   k_gather_sorted<<<dim3(gx, nc), 256, 0, s>>>(dcols, raw, doff, sv.perm, dcenter);
   k_thumb<<<(nc + 63) / 64, 64, 0, s>>>(dcols, raw, doff, dpw, dst, nc);
-  k_hest_init<<<(nc + 63) / 64, 64, 0, s>>>(dst, nc, (mode == 0 || mode == 2) ? dhin : nullptr,
-                                            mode == 2 ? skip : 0, mode == 0 ? 1 : 0);
+  k_hest_init<<<(nc + 63) / 64, 64, 0, s>>>(
+      dst, nc, (mode == 0 || (mode == 2 && !d_log_ratio)) ? dhin : nullptr,
+      mode == 2 ? skip : 0, mode == 0 ? 1 : 0, mode == 2 ? d_log_ratio : nullptr);
   k_conv_plan<<<(std::max(slots, 1u) + 127) / 128, 128, 0, s>>>(dcols, nc, dbase, dst,
                                                                  mode == 0 ? 1 : 0, tiles, slots,
                                                                  tt_used);
@@ -634,7 +644,7 @@ int hestimate_engine(Ctx& c, const float* raw, const std::vector<uint64_t>& raw_
       std::vector<float> h2(redo.size());
       std::vector<ent_hest_stats> st2(redo.size());
       int r2 = hestimate_engine(c, raw, off2, len2, 1, nullptr, 0, h2.data(), nullptr,
-                                st2.data());
+                                st2.data(), nullptr);
       if (r2) return r2;
       for (size_t q = 0; q < redo.size(); ++q) {
         h_out[redo[q]] = h2[q];
@@ -679,7 +689,8 @@ static int hest_common(ent_ctx* ctx, const float* coords, size_t n_rows, size_t 
     // h0 only: a zero-level search reports it
     std::vector<float> dummy(n_sel);
     std::vector<ent_hest_stats> st(n_sel);
-    s = hestimate_engine(c, raw, off, lens, 2, h_out, 64, dummy.data(), nullptr, st.data());
+    s = hestimate_engine(c, raw, off, lens, 2, h_out, 64, dummy.data(), nullptr, st.data(),
+                         nullptr);
     if (s) return s;
     for (size_t q = 0; q < n_sel; ++q) {
       h_out[q] = st[q].h0;
@@ -689,7 +700,8 @@ static int hest_common(ent_ctx* ctx, const float* coords, size_t n_rows, size_t 
       }
     }
   } else {
-    s = hestimate_engine(c, raw, off, lens, (int)mode, h_init, (int)skip, h_out, nullptr, stats);
+    s = hestimate_engine(c, raw, off, lens, (int)mode, h_init, (int)skip, h_out, nullptr, stats,
+                         nullptr);
     if (s) return s;
   }
   s = c.end_call();
@@ -714,7 +726,7 @@ int ent_epa_convolution(ent_ctx* ctx, const float* sorted, size_t n, float h, fl
   std::vector<uint64_t> off(1, 0);
   std::vector<uint32_t> lens(1, (uint32_t)n);
   float hv = h, dummy = 0.f;
-  s = hestimate_engine(c, p, off, lens, 0, &hv, 0, &dummy, out, nullptr);
+  s = hestimate_engine(c, p, off, lens, 0, &hv, 0, &dummy, out, nullptr, nullptr);
   if (s) return s;
   s = c.end_call();
   c.collect_kernel_stats();
@@ -734,6 +746,98 @@ int ent_hestimate_device(ent_ctx* ctx, const float* d_coords, size_t n_rows, siz
                          ent_hest_stats* stats) {
   return hest_common(ctx, d_coords, n_rows, n_cols, cols, n_sel, mode, h_init, skip_levels,
                      h_out, stats, true);
+}
+
+// Bandwidth search over every dimension of uneven instances: the full AMISE
+// search (net == nullptr) or the learned warm start.
+static int hest_instances(ent_ctx* ctx, ent_mlp* net, const ent_instance* inst, size_t n_inst,
+                          uint32_t flags, uint32_t skip_levels, float* h_out,
+                          ent_hest_stats* stats) {
+  if (!ctx || !inst || !h_out || n_inst == 0) return ENT_ERR_ARG;
+  Ctx& c = *reinterpret_cast<Ctx*>(ctx);
+  int s = c.begin_call();
+  if (s) return s;
+  const bool dev = (flags & ENT_BATCH_DEVICE_INPUT) != 0;
+  std::vector<const float*> base(n_inst);
+  std::vector<uint32_t> nn(n_inst), dd(n_inst);
+  std::vector<uint64_t> off;
+  std::vector<uint32_t> lens;
+  std::vector<uint32_t> col_inst, col_dim;
+  // all instance dimensions are columns of one device buffer region each
+  const float* raw0 = nullptr;
+  for (size_t q = 0; q < n_inst; ++q) {
+    if (inst[q].d < 1 || inst[q].d > 3) return c.fail(ENT_ERR_DIM, ent_status_string(ENT_ERR_DIM));
+    if (inst[q].n < 2 || inst[q].n > 0xffffff00ull) return c.fail(ENT_ERR_ARG, "bad size");
+    const float* p = inst[q].coords;
+    if (!dev) {
+      float* d = static_cast<float*>(c.arena.alloc(4 * inst[q].n * inst[q].d));
+      if (!d) return c.fail(ENT_ERR_CUDA, "out of device memory");
+      cudaError_t e = cudaMemcpyAsync(d, inst[q].coords, 4 * inst[q].n * inst[q].d,
+                                      cudaMemcpyHostToDevice, c.stream);
+      if (e != cudaSuccess) return c.cuda_fail(e, "copy coordinates");
+      p = d;
+    }
+    base[q] = p;
+    nn[q] = (uint32_t)inst[q].n;
+    dd[q] = inst[q].d;
+  }
+  // offsets relative to the lowest address so one raw pointer covers all
+  raw0 = *std::min_element(base.begin(), base.end());
+  for (size_t q = 0; q < n_inst; ++q)
+    for (uint32_t j = 0; j < dd[q]; ++j) {
+      off.push_back((uint64_t)(base[q] - raw0) + (uint64_t)j * nn[q]);
+      lens.push_back(nn[q]);
+      col_inst.push_back((uint32_t)q);
+      col_dim.push_back(j);
+    }
+  std::vector<float> hc(lens.size());
+  std::vector<ent_hest_stats> sc(lens.size());
+  if (net) {
+    float* df = static_cast<float*>(c.arena.alloc(4 * 32 * n_inst));
+    float* dy = static_cast<float*>(c.arena.alloc(4 * 3 * n_inst));
+    float* dr = static_cast<float*>(c.arena.alloc(4 * lens.size()));
+    if (!df || !dy || !dr) return c.fail(ENT_ERR_CUDA, "out of device memory");
+    s = mlp_features_device(c, base, nn, dd, df);
+    if (s) return s;
+    s = mlp_forward_device(c, net, df, n_inst, dy);
+    if (s) return s;
+    // per column: r = y[inst][dim]
+    std::vector<uint32_t> map(lens.size());
+    for (size_t k = 0; k < lens.size(); ++k) map[k] = col_inst[k] * 3 + col_dim[k];
+    cudaError_t e;
+    uint32_t* dmap = upload(c, map, &e);
+    if (e != cudaSuccess) return c.cuda_fail(e, "upload map");
+    k_pick<<<(unsigned)((lens.size() + 127) / 128), 128, 0, c.stream>>>(dy, dmap, dr,
+                                                                       (uint32_t)lens.size());
+    c.stats.kernel_launches += 1;
+    s = hestimate_engine(c, raw0, off, lens, 2, nullptr, (int)skip_levels, hc.data(), nullptr,
+                         sc.data(), dr);
+  } else {
+    s = hestimate_engine(c, raw0, off, lens, 1, nullptr, 0, hc.data(), nullptr, sc.data(),
+                         nullptr);
+  }
+  if (s) return s;
+  for (size_t q = 0; q < n_inst; ++q)
+    for (int j = 0; j < 3; ++j) h_out[3 * q + j] = 0.f;
+  for (size_t k = 0; k < lens.size(); ++k) {
+    h_out[3 * col_inst[k] + col_dim[k]] = hc[k];
+    if (stats) stats[3 * col_inst[k] + col_dim[k]] = sc[k];
+  }
+  s = c.end_call();
+  c.collect_kernel_stats();
+  return s;
+}
+
+int ent_hestimate_learned(ent_ctx* ctx, ent_mlp* net, const ent_instance* inst, size_t n_inst,
+                          uint32_t flags, uint32_t skip_levels, float* h_out,
+                          ent_hest_stats* stats) {
+  if (!net) return ENT_ERR_ARG;
+  return hest_instances(ctx, net, inst, n_inst, flags, skip_levels, h_out, stats);
+}
+
+int ent_hestimate_batch(ent_ctx* ctx, const ent_instance* inst, size_t n_inst, uint32_t flags,
+                        float* h_out, ent_hest_stats* stats) {
+  return hest_instances(ctx, nullptr, inst, n_inst, flags, 0, h_out, stats);
 }
 
 }  // extern "C"

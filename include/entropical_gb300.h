@@ -247,6 +247,63 @@ int ent_hestimate_device(ent_ctx* ctx, const float* d_coords, size_t n_rows,
                          uint32_t skip_levels, float* h_out,
                          ent_hest_stats* stats);
 
+/*
+ * Full AMISE search (ENT_HEST_AMISE) for every dimension of uneven
+ * instances in one batch; h_out, stats: n_inst x 3 (slots beyond d zero).
+ * flags: ENT_BATCH_DEVICE_INPUT for device coordinates.
+ */
+int ent_hestimate_batch(ent_ctx* ctx, const ent_instance* inst, size_t n_inst,
+                        uint32_t flags, float* h_out, ent_hest_stats* stats);
+
+/* --------------------------------------- learned bandwidth warm start */
+
+/*
+ * A small MLP (32 -> 128 -> 128 -> 3, ReLU; 21,123 parameters) trained and
+ * run by this library's own kernels: BF16 weights in the passes, FP32
+ * accumulation, FP32 master weights and Adam moments on the device. It maps
+ * 32 summary features of an instance (ent_features) to r_j =
+ * log(h_j / h0_j) per dimension j, the AMISE bandwidth relative to the rule
+ * of thumb, which warm-starts the AMISE search. No counterpart in the
+ * reference beyond the search it shortens (hestimate.cpp:55-104).
+ */
+typedef struct ent_mlp ent_mlp;
+
+size_t ent_mlp_param_count(void);
+int ent_mlp_create(ent_ctx* ctx, uint64_t seed, ent_mlp** net);
+void ent_mlp_destroy(ent_mlp* net);
+/* Flat FP32 parameters [W1 128x32, b1, W2 128x128, b2, W3 3x128, b3] and
+ * the feature normalisation (32 means, 32 scales); any pointer may be NULL. */
+int ent_mlp_set_params(ent_mlp* net, const float* params, const float* feat_mu,
+                       const float* feat_sd);
+int ent_mlp_get_params(const ent_mlp* net, float* params, float* feat_mu,
+                       float* feat_sd);
+/* Y[B x 3] for raw (unnormalised) features X[B x 32]; host memory. */
+int ent_mlp_forward(ent_ctx* ctx, ent_mlp* net, const float* X, size_t B,
+                    float* Y);
+/* Gradient of the masked mean-squared error sum(mask (Y - T)^2) / sum(mask)
+ * with respect to the flat parameters (no update); host memory. */
+int ent_mlp_gradients(ent_ctx* ctx, ent_mlp* net, const float* X,
+                      const float* T, const float* mask, size_t B,
+                      float* grads, float* loss);
+/* One Adam step (beta 0.9 / 0.999) on a batch; *loss before the step. */
+int ent_mlp_train_step(ent_ctx* ctx, ent_mlp* net, const float* X,
+                       const float* T, const float* mask, size_t B, float lr,
+                       float* loss);
+/* The 32 features of every instance (feat: n_inst x 32); host memory. */
+int ent_features(ent_ctx* ctx, const ent_instance* inst, size_t n_inst,
+                 float* feat);
+/*
+ * Per-dimension AMISE bandwidths of every instance dimension, each search
+ * entered skip_levels levels deep at the node of h0 * exp(r) predicted by
+ * the network (features, network and search all on the device), falling
+ * back to the full search where the warm search ends against an inner node
+ * edge. h_out, stats: n_inst x 3 (slots beyond d are zero).
+ * flags: ENT_BATCH_DEVICE_INPUT for device coordinates.
+ */
+int ent_hestimate_learned(ent_ctx* ctx, ent_mlp* net, const ent_instance* inst,
+                          size_t n_inst, uint32_t flags, uint32_t skip_levels,
+                          float* h_out, ent_hest_stats* stats);
+
 #ifdef __cplusplus
 }
 #endif
