@@ -74,14 +74,16 @@ __global__ void k_thumb(const ConvCol* __restrict__ cols, const float* __restric
   st[c].n = n;
 }
 
+// raw_off: offset of each column in the raw coordinates; perm_off: offset of
+// its value order in the sort permutation (laid out by view, not by column).
 __global__ void k_gather_sorted(const ConvCol* __restrict__ cols,
                                 const float* __restrict__ raw,
                                 const uint64_t* __restrict__ raw_off,
                                 const uint32_t* __restrict__ perm,
-                                const float* __restrict__ center) {
+                                const uint64_t* __restrict__ perm_off) {
   const ConvCol& C = cols[blockIdx.y];
   const float* x = raw + raw_off[blockIdx.y];
-  const uint32_t* p = perm + raw_off[blockIdx.y];
+  const uint32_t* p = perm + perm_off[blockIdx.y];
   float* xs = const_cast<float*>(C.xs);
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < C.n + 8;
        k += gridDim.x * blockDim.x)
@@ -520,7 +522,6 @@ int hestimate_engine(Ctx& c, const float* raw, const std::vector<uint64_t>& raw_
   const uint32_t tt_used = mode == 0 ? Cfg<1, CONV_R1>::TT : Cfg<1, CONV_R2>::TT;
   uint32_t slots = 0;
   std::vector<uint32_t> base(nc);
-  std::vector<float> center(nc);
   std::vector<double> pw(nc);
   for (uint32_t i = 0; i < nc; ++i) {
     hc[i].n = lens[i];
@@ -530,15 +531,14 @@ int hestimate_engine(Ctx& c, const float* raw, const std::vector<uint64_t>& raw_
     hc[i].tile_base = slots;
     base[i] = slots;
     slots += hc[i].n_tiles;
-    center[i] = 0.5f * (sv.stats[i].mn + sv.stats[i].mx);
     pw[i] = std::pow((double)lens[i], -1.0 / 7.0);  // std::pow(n_rows, -1/7)
   }
   ConvCol* dcols = upload(c, hc, &e);
   if (e != cudaSuccess) return c.cuda_fail(e, "upload columns");
   uint64_t* doff = upload(c, raw_off, &e);
   if (e != cudaSuccess) return c.cuda_fail(e, "upload offsets");
-  float* dcenter = upload(c, center, &e);
-  if (e != cudaSuccess) return c.cuda_fail(e, "upload centres");
+  uint64_t* dpoff = upload(c, sv.off, &e);
+  if (e != cudaSuccess) return c.cuda_fail(e, "upload permutation offsets");
   double* dpw = upload(c, pw, &e);
   if (e != cudaSuccess) return c.cuda_fail(e, "upload powers");
   uint32_t* dbase = upload(c, base, &e);
@@ -558,7 +558,7 @@ int hestimate_engine(Ctx& c, const float* raw, const std::vector<uint64_t>& raw_
   cudaMemsetAsync(dst, 0, sizeof(HestState) * nc, s);
 
   const unsigned gx = std::min<uint32_t>((std::max(sv.max_n, 1u) + 255) / 256 + 1, 1024);
-  k_gather_sorted<<<dim3(gx, nc), 256, 0, s>>>(dcols, raw, doff, sv.perm, dcenter);
+  k_gather_sorted<<<dim3(gx, nc), 256, 0, s>>>(dcols, raw, doff, sv.perm, dpoff);
   k_thumb<<<(nc + 63) / 64, 64, 0, s>>>(dcols, raw, doff, dpw, dst, nc);
   k_hest_init<<<(nc + 63) / 64, 64, 0, s>>>(
       dst, nc, (mode == 0 || (mode == 2 && !d_log_ratio)) ? dhin : nullptr,

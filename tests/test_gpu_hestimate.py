@@ -57,3 +57,31 @@ def test_warm_start_saves_levels_and_is_exact(ctx):
     bad, sb = ctx.hestimate(cols, HEST_AMISE_WARM, h_init=0.3 * h0, skip_levels=6)
     assert np.array_equal(bad, full)
     assert all(s["warm_converged"] == 0 and s["conv_evals"] == 20 for s in sb)
+
+
+def test_hestimate_device_column_subset(ctx):
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(21)
+    cols = np.stack([workloads.mixture_instance(rng, 1, 7000)[0] for _ in range(5)])
+    full, _ = ctx.hestimate(cols, HEST_AMISE)
+    d = torch.from_numpy(cols).cuda()
+    sel = np.array([4, 1, 3], np.uint32)
+    h = np.zeros(3, np.float32)
+    import ctypes as C
+    from entropical_gb300._native import HestStats, c_f32_p, c_u32_p
+    st = (HestStats * 3)()
+    ctx.check(ctx.lib.ent_hestimate_device(ctx.handle, C.c_void_p(d.data_ptr()), 7000, 5,
+                                           sel.ctypes.data_as(c_u32_p), 3, HEST_AMISE, None, 0,
+                                           h.ctypes.data_as(c_f32_p), C.cast(st, C.c_void_p)))
+    assert np.array_equal(h, full[sel])
+
+
+def test_hestimate_instance_batch(ctx):
+    from entropical_gb300 import learned
+    rng = np.random.default_rng(22)
+    items = [workloads.mixture_instance(rng, d, n) for d, n in [(2, 4000), (1, 9000), (3, 3000)]]
+    h, st = learned.hestimate_full(ctx, items)
+    for q, x in enumerate(items):
+        ref, _ = ctx.hestimate(x, HEST_AMISE)
+        assert np.array_equal(h[q, :x.shape[0]], ref)
+        assert np.all(h[q, x.shape[0]:] == 0)
