@@ -87,6 +87,8 @@ SIGNATURES: dict[str, tuple] = {
     "ent_mlp_train_step": (C.c_int, [C.c_void_p, C.c_void_p, c_f32_p, c_f32_p, c_f32_p,
                                      C.c_size_t, C.c_float, c_f32_p]),
     "ent_features": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, c_f32_p]),
+    "ent_density_1d_noalloc": (C.c_int, [C.c_void_p, C.c_size_t, C.c_float, C.c_void_p,
+                                         C.c_void_p]),
     "ent_epa_convolution": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_float, c_f32_p]),
     "ent_hestimate": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, c_u32_p,
                                 C.c_size_t, C.c_uint32, c_f32_p, C.c_uint32, c_f32_p,

@@ -255,6 +255,29 @@ int ent_hestimate_device(ent_ctx* ctx, const float* d_coords, size_t n_rows,
 int ent_hestimate_batch(ent_ctx* ctx, const ent_instance* inst, size_t n_inst,
                         uint32_t flags, float* h_out, ent_hest_stats* stats);
 
+/* ------------------------------------------- allocation-free density */
+
+/* Largest input of ent_density_1d_noalloc. */
+#define ENT_NOALLOC_MAX_N 65536u
+
+/*
+ * The 1-D density of ent_densities_device (one column, no lag, divided by
+ * n) for callers that cannot allocate device memory -- for instance when
+ * another framework owns the device memory pool, or in a service that must
+ * not allocate after start-up. No counterpart in the reference, which
+ * allocated and freed device memory on every call (density_1d.cuh:108-164).
+ * All working memory is one fixed 2 MiB device array inside this library
+ * (held on every device that loads it until the process exits), so n must
+ * not exceed ENT_NOALLOC_MAX_N (ENT_ERR_TOO_LARGE otherwise). d_x (n floats)
+ * and d_out (n doubles) are device memory of the current device; stream may
+ * be NULL. The call is synchronous and calls no allocator. The first call on
+ * a device looks up the array's device address and should come before any
+ * stream capture. Calls share the array: calls that overlap on the GPU race
+ * and must be serialised by the caller.
+ */
+int ent_density_1d_noalloc(const float* d_x, size_t n, float h, double* d_out,
+                           void* stream);
+
 /* --------------------------------------- learned bandwidth warm start */
 
 /*
