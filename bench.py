@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-compare", action="store_true",
+                    help="skip the batched+learned vs plain comparison")
     ap.add_argument("--coords", type=int, default=N_COORDS,
                     help="coordinates of the MI batch (64 = the benchmark workload; "
                          "smaller values give the small case used for ncu captures)")
@@ -147,6 +149,75 @@ def cpu_port_sample(x: np.ndarray, h: np.ndarray, pairs, support):
         O.density_ref_f32(O.repack(x, list(inst)), [h[c] for c in inst], linear_scan=True)
     dt = time.perf_counter() - t0
     return support / dt, dt
+
+
+def compare_plain(ctx, x, ptr, log_fp64_pairs=2):
+    """Bandwidths by the AMISE search and then all-pairs MI, two ways:
+    plain  -- the single-instance entry points called the way the reference
+              calls them: per column 16 epa_convolution calls driven by the
+              AmiseMin bracket logic (hestimate.cpp:55-104), then mi.cpp's loop
+              (per pair the 1-D marginal again and the 2-D joint, mi.cpp:37-59);
+    batched+learned -- ent_hestimate_learned (features, network, warm search
+              for all columns at once) and one ent_mi_all_pairs batch.
+    Returns a dict of times, convolution counts and MI differences."""
+    from entropical_gb300 import learned
+    from entropical_gb300.densities import HEST_THUMB
+    from entropical_gb300.estimators import hestimate_amise_plain
+    M, N = x.shape
+    torch_sync = __import__("torch").cuda.synchronize
+    torch_sync()
+    t0 = time.perf_counter()
+    h0, _ = ctx.hestimate(x, HEST_THUMB)
+    h_plain, calls = np.zeros(M, np.float32), 0
+    for j in range(M):
+        hj, c = hestimate_amise_plain(ctx, x[j], float(h0[j]))
+        h_plain[j], calls = hj, calls + c
+    t_hest_plain = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    mi_plain = np.zeros((M, M))
+    for i in range(M):
+        Hi = -np.mean(np.log(ctx.combined_densities(x, None, [i], [h_plain[i]])))
+        for j in range(i + 1, M):
+            Hj = -np.mean(np.log(ctx.combined_densities(x, None, [j], [h_plain[j]])))
+            Hij = -np.mean(np.log(ctx.combined_densities(x, None, [i, j],
+                                                         [h_plain[i], h_plain[j]])))
+            mi_plain[i, j] = mi_plain[j, i] = Hi + Hj - Hij
+    t_mi_plain = time.perf_counter() - t0
+    net = learned.BandwidthMLP.load(ctx)
+    items = [(ptr + 4 * N * j, 1, N) for j in range(M)]
+    learned.hestimate_learned(ctx, net, items, skip_levels=6, device=True)  # warm-up
+    torch_sync()
+    t0 = time.perf_counter()
+    hl, st = learned.hestimate_learned(ctx, net, items, skip_levels=6, device=True)
+    t_hest_l = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    mi_b, _ = ctx.mi_all_pairs_device(ptr, N, M, hl[:, 0])
+    t_mi_b = time.perf_counter() - t0
+    iu = np.triu_indices(M, 1)
+    out = {
+        "workload": "AMISE bandwidths for 64 columns, then all-pairs MI (64 x 100k)",
+        "plain_s": t_hest_plain + t_mi_plain, "plain_hestimate_s": t_hest_plain,
+        "plain_mi_s": t_mi_plain, "plain_density_calls": M + 2 * len(iu[0]),
+        "plain_conv_calls": calls,
+        "batched_learned_s": t_hest_l + t_mi_b, "learned_hestimate_s": t_hest_l,
+        "batched_mi_s": t_mi_b,
+        "learned_conv_evals": int(sum(s[0]["conv_evals"] for s in st)),
+        "learned_fallbacks": int(sum(1 - s[0]["warm_converged"] for s in st)),
+        "bandwidths_identical": bool(np.array_equal(hl[:, 0], h_plain)),
+        "max_abs_dI_batched_vs_plain": float(np.max(np.abs(mi_b - mi_plain)[iu])),
+    }
+    out["speedup"] = out["plain_s"] / out["batched_learned_s"]
+    try:
+        from oracle import oracle as O
+        errs = []
+        for (i, j) in [(0, 1), (5, 40)][:log_fp64_pairs]:
+            ref = O.mi_fp64(x[i], x[j], float(h_plain[i]), float(h_plain[j]))
+            errs.append(abs(mi_b[i, j] - ref))
+        out["max_abs_dI_vs_fp64_oracle"] = max(errs)
+        out["fp64_oracle_pairs"] = log_fp64_pairs
+    except Exception as exc:
+        out["fp64_oracle_error"] = str(exc)[:200]
+    return out
 
 
 def reference_arm(args, x, h):
@@ -290,6 +361,11 @@ def main():
                      "kernel": "k_density<2,16> (2-D pair kernel)",
                      "flops_per_pair": 10, "peak_kind": peak_note},
     }
+    if not args.no_compare and ws == 1:
+        try:
+            line["batched_learned_vs_plain"] = compare_plain(ctx, x, ptr)
+        except Exception as exc:
+            line["batched_learned_vs_plain"] = {"error": str(exc)[:300]}
     if not args.no_cpu_baseline and ws == 1:
         try:
             from oracle import oracle as O

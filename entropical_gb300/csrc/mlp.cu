@@ -34,6 +34,7 @@ using namespace ent;
 namespace {
 
 constexpr int NI = 32, NH = 128, NO = 3;
+constexpr float FEAT_CLIP = 6.f;
 constexpr size_t OFF_W1 = 0, OFF_B1 = OFF_W1 + NH * NI, OFF_W2 = OFF_B1 + NH,
                  OFF_B2 = OFF_W2 + NH * NH, OFF_W3 = OFF_B2 + NH, OFF_B3 = OFF_W3 + NO * NH,
                  N_PARAMS = OFF_B3 + NO;  // 21,123
@@ -233,7 +234,9 @@ __global__ void k_normalize(float* __restrict__ X, const float* __restrict__ mu,
                             const float* __restrict__ sd, int B) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B * NI; i += gridDim.x * blockDim.x) {
     const int f = i % NI;
-    X[i] = (X[i] - mu[f]) / sd[f];
+    // standardised and clipped: heavy-tailed features (kurtosis of narrow
+    // mixtures) must not dominate the first layer
+    X[i] = fminf(fmaxf((X[i] - mu[f]) / sd[f], -FEAT_CLIP), FEAT_CLIP);
   }
 }
 
@@ -400,7 +403,9 @@ int ent_mlp_create(ent_ctx* ctx, uint64_t seed, ent_mlp** out) {
   std::normal_distribution<float> nd(0.f, 1.f);
   for (size_t i = 0; i < (size_t)NH * NI; ++i) p[OFF_W1 + i] = nd(rng) * std::sqrt(2.f / NI);
   for (size_t i = 0; i < (size_t)NH * NH; ++i) p[OFF_W2 + i] = nd(rng) * std::sqrt(2.f / NH);
-  for (size_t i = 0; i < (size_t)NO * NH; ++i) p[OFF_W3 + i] = nd(rng) * std::sqrt(1.f / NH);
+  // the output layer starts at zero: the network begins as the constant
+  // predictor b3 and opens its feature paths only where they reduce the loss
+  for (size_t i = 0; i < (size_t)NO * NH; ++i) p[OFF_W3 + i] = 0.f;
   std::vector<float> mu(NI, 0.f), sd(NI, 1.f);
   cudaMemcpy(n->p, p.data(), 4 * N_PARAMS, cudaMemcpyHostToDevice);
   cudaMemset(n->m, 0, 4 * N_PARAMS);

@@ -225,7 +225,12 @@ def train(ctx: Context, X, T, M, epochs: int = 30, batch: int = 256, lr: float =
     """Train a fresh network with the device Adam step; returns (net, losses)."""
     net = BandwidthMLP(ctx, seed)
     mu, sd = normalisation(X)
-    net.set_params(None, mu, sd)
+    # output biases start at the mean target of each output
+    p, _, _ = net.get_params()
+    for j in range(NO):
+        sel = M[:, j] > 0
+        p[p.size - NO + j] = float(T[sel, j].mean()) if sel.any() else 0.0
+    net.set_params(p, mu, sd)
     rng = np.random.default_rng(seed)
     losses = []
     for ep in range(epochs):
@@ -247,10 +252,20 @@ def main(argv=None):
     ap.add_argument("--epochs", type=int, default=30)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--out", default=str(DEFAULT_WEIGHTS))
+    ap.add_argument("--dataset", default=None,
+                    help="npz of (X, T, M): loaded if it exists, else generated and saved")
+    ap.add_argument("--lr", type=float, default=1e-3)
     args = ap.parse_args(argv)
     ctx = Context(0)
-    X, T, M = make_dataset(ctx, args.n_mix, args.seed, log=print)
-    net, losses = train(ctx, X, T, M, epochs=args.epochs, log=print)
+    if args.dataset and Path(args.dataset).exists():
+        z = np.load(args.dataset)
+        X, T, M = z["X"], z["T"], z["M"]
+    else:
+        X, T, M = make_dataset(ctx, args.n_mix, args.seed, log=print)
+        if args.dataset:
+            np.savez_compressed(args.dataset, X=X, T=T, M=M)
+    print("labels r: mean", float(T[M > 0].mean()), "sd", float(T[M > 0].std()))
+    net, losses = train(ctx, X, T, M, epochs=args.epochs, lr=args.lr, log=print)
     Path(args.out).parent.mkdir(parents=True, exist_ok=True)
     net.save(args.out)
     print("saved", args.out, "final loss", losses[-1])

@@ -4,7 +4,8 @@ Used by tests/ to check the gradients and outputs of the CUDA MLP kernels.
 The network is 32 -> 128 -> 128 -> 3 with ReLU; the flat parameter layout is
 [W1 (128x32), b1, W2 (128x128), b2, W3 (3x128), b3]. The CUDA passes use the
 weights rounded to BF16 (biases stay FP32) on inputs normalised as
-(x - mu) / sd, so this reference does the same, in FP64 otherwise. Loss:
+(x - mu) / sd and clipped to [-6, 6], so this reference does the same, in
+FP64 otherwise. Loss:
 sum(mask (y - t)^2) / sum(mask). Also restates the 32 summary features.
 """
 from __future__ import annotations
@@ -41,7 +42,7 @@ def forward(p, mu, sd, X):
     W1, W2, W3 = (bf16(w[k]).astype(np.float64) for k in ("W1", "W2", "W3"))
     b1, b2, b3 = (w[k].astype(np.float64) for k in ("b1", "b2", "b3"))
     x = (np.asarray(X, np.float32) - mu) / sd
-    x = x.astype(np.float32).astype(np.float64)
+    x = np.clip(x.astype(np.float32), -6.0, 6.0).astype(np.float64)
     z1 = x @ W1.T + b1
     h1 = np.maximum(z1, 0)
     z2 = h1 @ W2.T + b2
