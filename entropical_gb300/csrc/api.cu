@@ -273,7 +273,7 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
         I.x[j] = views[s.view[j]].x;
         // exact power-of-two scale with g = h 2^k in [1, 2), limited so that
         // no scaled coordinate can overflow
-        int k = -std::ilogb(s.h[j]);
+        int k = -std::ilogb(s.h[j]) - 1;  // g in [0.5, 1): g^2 - d^2 < 1
         const double amax = std::max(std::fabs((double)st_j.mn), std::fabs((double)st_j.mx));
         while (k > -126 && amax * std::ldexp(1.0, k) > 1e37) --k;
         k = std::max(-126, std::min(126, k));
@@ -419,7 +419,10 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
     if (group_slots[d] == 0) continue;
     int launched = 0;
     cudaEventRecord(c.ev_d[d - 1][0], st);
-    e = launch_density(st, d, c.tile_r[d - 1], tiles + group_base[d], group_slots[d], di_sorted,
+    e = launch_density(st, d, c.tile_r[d - 1],
+                       density_variant_supported(d, c.tile_r[d - 1], c.pair_variant)
+                           ? c.pair_variant : 0,
+                       tiles + group_base[d], group_slots[d], di_sorted,
                        wc + d, c.d_err, tile_ls + group_base[d], mode, c.n_sms,
                        &launched);
     if (e != cudaSuccess) return c.cuda_fail(e, "density kernel");
@@ -558,6 +561,8 @@ int ent_set_tuning(ent_ctx* ctx, const ent_tuning* t) {
     if (t->targets_per_warp[d - 1] && !density_r_supported(d, (int)t->targets_per_warp[d - 1]))
       return c->fail(ENT_ERR_ARG, "unsupported targets_per_warp");
   if (t->cells_per_h > 4) return c->fail(ENT_ERR_ARG, "cells_per_h must be 1..4");
+  if (t->pair_variant > 2) return c->fail(ENT_ERR_ARG, "pair_variant must be 0..2");
+  if (t->pair_variant) c->pair_variant = (int)t->pair_variant - 1;
   for (int d = 1; d <= 3; ++d)
     if (t->targets_per_warp[d - 1]) c->tile_r[d - 1] = (int)t->targets_per_warp[d - 1];
   if (t->cells_per_h) c->strip_subdiv = t->cells_per_h;
@@ -569,6 +574,7 @@ int ent_get_tuning(const ent_ctx* ctx, ent_tuning* t) {
   const Ctx* c = reinterpret_cast<const Ctx*>(ctx);
   for (int d = 0; d < 3; ++d) t->targets_per_warp[d] = (uint32_t)c->tile_r[d];
   t->cells_per_h = c->strip_subdiv;
+  t->pair_variant = (uint32_t)c->pair_variant + 1;
   return ENT_OK;
 }
 

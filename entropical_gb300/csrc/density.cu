@@ -319,7 +319,7 @@ __global__ void k_plan(const InstDev* __restrict__ insts, uint32_t n_inst,
 }
 
 // ------------------------------------------------------- pair kernel
-template <int D, int R>
+template <int D, int R, int V>
 __global__ void __launch_bounds__(128)
     k_density(const TileDesc* __restrict__ tiles, uint32_t n_slots,
               const InstDev* __restrict__ insts, uint32_t* work_counter,
@@ -455,6 +455,63 @@ __global__ void __launch_bounds__(128)
             }
 #pragma unroll
             for (int r = 0; r < R; ++r) kahan_add(ks[r], kc[r], acc[r]);
+          } else if constexpr (V == 1) {
+            // saturating body: (g^2 - d^2)^+ = sat(fma(-d, d, g^2)) because
+            // g^2 < 1; all work on the FMA pipe, no min on the ALU
+            const float g2a = -ng0, g2b = -ng1, g2c = -ng2;
+            if constexpr (D == 1) {
+              f32x2 acc[R / 2];
+              f32x2 T[R / 2];
+#pragma unroll
+              for (int i = 0; i < R / 2; ++i) {
+                acc[i] = pk2(0.f, 0.f);
+                T[i] = pk2(T2[2 * i], T2[2 * i + 1]);
+              }
+#pragma unroll 2
+              for (uint32_t k = lane; k < n; k += 32) {
+                const float s = B[s0 + k];
+                const f32x2 S = pk2(s, s);
+#pragma unroll
+                for (int i = 0; i < R / 2; ++i) {
+                  float da, db;
+                  upk2(sub2(T[i], S), da, db);
+                  acc[i] = add2(acc[i], pk2(__saturatef(__fmaf_rn(-da, da, g2a)),
+                                            __saturatef(__fmaf_rn(-db, db, g2a))));
+                }
+              }
+#pragma unroll
+              for (int i = 0; i < R / 2; ++i) {
+                float a0, a1;
+                upk2(acc[i], a0, a1);
+                kahan_add(ks[2 * i], kc[2 * i], a0);
+                kahan_add(ks[2 * i + 1], kc[2 * i + 1], a1);
+              }
+            } else {
+              float acc[R];
+#pragma unroll
+              for (int r = 0; r < R; ++r) acc[r] = 0.f;
+#pragma unroll 2
+              for (uint32_t k = lane; k < n; k += 32) {
+                const P s = B[s0 + k];
+                const f32x2 S = pk2(s.x, s.y);
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                  float dx, dy;
+                  upk2(sub2(T01[r], S), dx, dy);
+                  const float wx = __saturatef(__fmaf_rn(-dx, dx, g2a));
+                  const float wy = __saturatef(__fmaf_rn(-dy, dy, g2b));
+                  if constexpr (D == 2) {
+                    acc[r] = __fmaf_rn(wx, wy, acc[r]);
+                  } else {
+                    const float dz = T2[r] - s.z;
+                    const float wz = __saturatef(__fmaf_rn(-dz, dz, g2c));
+                    acc[r] = __fmaf_rn(wx * wy, wz, acc[r]);
+                  }
+                }
+              }
+#pragma unroll
+              for (int r = 0; r < R; ++r) kahan_add(ks[r], kc[r], acc[r]);
+            }
           } else if constexpr (D == 1) {
             f32x2 acc[R / 2];
             f32x2 T[R / 2];
@@ -576,14 +633,14 @@ __global__ void __launch_bounds__(128)
   }
 }
 
-template <int D, int R>
+template <int D, int R, int V>
 cudaError_t launch_density_t(cudaStream_t st, const TileDesc* tiles,
                              uint32_t n_slots, const InstDev* insts,
                              uint32_t* work_counter, uint32_t* err,
                              double* tile_logsum, uint32_t mode, int n_sms,
                              int* launched) {
   typedef Cfg<D, R> C;
-  auto kern = k_density<D, R>;
+  auto kern = k_density<D, R, V>;
   cudaError_t e = cudaFuncSetAttribute(
       kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM);
   if (e != cudaSuccess) return e;
@@ -627,6 +684,11 @@ __global__ void __launch_bounds__(256)
 }  // namespace
 
 // Targets per warp: the tunable variants of each dimension (tile = 4 warps).
+int density_variant_supported(int d, int r, int v) {
+  if (v == 0) return density_r_supported(d, r);
+  return v == 1 && r == (d == 3 ? 8 : 16);
+}
+
 int density_r_supported(int d, int r) {
   if (d == 1 || d == 2) return r == 8 || r == 16;
   if (d == 3) return r == 4 || r == 8;
@@ -698,23 +760,35 @@ cudaError_t launch_plan(cudaStream_t st, const InstDev* insts, uint32_t n_inst,
   return cudaGetLastError();
 }
 
+cudaError_t launch_density(cudaStream_t st, int d, int r, int v, const TileDesc* tiles,
+                           uint32_t n_slots, const InstDev* insts,
+                           uint32_t* work_counter, uint32_t* err,
+                           double* tile_logsum, uint32_t mode, int n_sms,
+                           int* launched) {
+#define ENT_LAUNCH(D, R, V)                                                         \
+  if (d == D && r == R && v == V)                                                   \
+    return launch_density_t<D, R, V>(st, tiles, n_slots, insts, work_counter, err,  \
+                                     tile_logsum, mode, n_sms, launched);
+  ENT_LAUNCH(1, 8, 0)
+  ENT_LAUNCH(1, 16, 0)
+  ENT_LAUNCH(1, 16, 1)
+  ENT_LAUNCH(2, 8, 0)
+  ENT_LAUNCH(2, 16, 0)
+  ENT_LAUNCH(2, 16, 1)
+  ENT_LAUNCH(3, 4, 0)
+  ENT_LAUNCH(3, 8, 0)
+  ENT_LAUNCH(3, 8, 1)
+#undef ENT_LAUNCH
+  return cudaErrorInvalidValue;
+}
+
 cudaError_t launch_density(cudaStream_t st, int d, int r, const TileDesc* tiles,
                            uint32_t n_slots, const InstDev* insts,
                            uint32_t* work_counter, uint32_t* err,
                            double* tile_logsum, uint32_t mode, int n_sms,
                            int* launched) {
-#define ENT_LAUNCH(D, R)                                                            \
-  if (d == D && r == R)                                                             \
-    return launch_density_t<D, R>(st, tiles, n_slots, insts, work_counter, err,     \
-                                  tile_logsum, mode, n_sms, launched);
-  ENT_LAUNCH(1, 8)
-  ENT_LAUNCH(1, 16)
-  ENT_LAUNCH(2, 8)
-  ENT_LAUNCH(2, 16)
-  ENT_LAUNCH(3, 4)
-  ENT_LAUNCH(3, 8)
-#undef ENT_LAUNCH
-  return cudaErrorInvalidValue;
+  return launch_density(st, d, r, 0, tiles, n_slots, insts, work_counter, err, tile_logsum,
+                        mode, n_sms, launched);
 }
 
 cudaError_t launch_inst_logsum(cudaStream_t st, const InstDev* insts,

@@ -52,7 +52,7 @@ struct InstDev {
   uint32_t tile_base, tile_cap;
   float lo1, lo2;           // cell-grid origins
   double inv_w1, inv_w2;    // inverse cell widths (cell width = h/S, widened)
-  float sc[3];  // exact power-of-two scale 2^k_j with g_j = h_j 2^k_j in [1, 2)
+  float sc[3];  // exact power-of-two scale 2^k_j with g_j = h_j 2^k_j in [0.5, 1)
   float g2[3];  // g_j^2: the support radius squared in scaled units
   const uint32_t* perm0;    // dimension-0 sorted order (view sort)
   uint32_t* perm;           // final strip-major order
@@ -102,6 +102,13 @@ cudaError_t launch_gather_pts(cudaStream_t st, const InstDev* insts,
 cudaError_t launch_plan(cudaStream_t st, const InstDev* insts, uint32_t n_inst,
                         const uint32_t* inst_tile_base, TileDesc* tiles,
                         uint32_t n_slots, uint64_t* n_src_total);
+// v: pair body, 0 = min-based, 1 = saturating FMA (needs g^2 < 1)
+cudaError_t launch_density(cudaStream_t st, int d, int r, int v, const TileDesc* tiles,
+                           uint32_t n_slots, const InstDev* insts,
+                           uint32_t* work_counter, uint32_t* err,
+                           double* tile_logsum, uint32_t mode, int n_sms,
+                           int* launched_ctas);
+// the original (min-based) pair body
 cudaError_t launch_density(cudaStream_t st, int d, int r, const TileDesc* tiles,
                            uint32_t n_slots, const InstDev* insts,
                            uint32_t* work_counter, uint32_t* err,
@@ -109,6 +116,7 @@ cudaError_t launch_density(cudaStream_t st, int d, int r, const TileDesc* tiles,
                            int* launched_ctas);
 // targets per warp R available for dimension d; tile = 4 warps x R targets
 int density_r_supported(int d, int r);
+int density_variant_supported(int d, int r, int v);
 int density_tile_targets(int d, int r);
 cudaError_t launch_inst_logsum(cudaStream_t st, const InstDev* insts,
                                uint32_t n_inst, const double* tile_logsum,

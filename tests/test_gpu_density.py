@@ -176,3 +176,21 @@ def test_mi_config_pair_sampled(ctx):
     t = np.random.default_rng(0).choice(100_000, 3000, replace=False)
     f = O.density_fp64(O.repack(x, [2, 5]), [h[2], h[5]], targets=t)
     assert rel_err(p[t], f) < REL
+
+
+@pytest.mark.parametrize("variant", [0, 1])
+@pytest.mark.parametrize("d", [1, 2, 3])
+def test_pair_body_variants(d, variant):
+    from entropical_gb300 import Context
+    rng = np.random.default_rng(60 + d)
+    x = rng.standard_normal((3, 6000)).astype(np.float32)
+    h = [0.2, 0.3, 0.25][:d]
+    cols = [2, 0, 1][:d]
+    with Context(0) as c:
+        c.set_tuning(pair_variant=variant)
+        assert c.tuning()["pair_variant"] == variant
+        p = c.combined_densities(x, None, cols, h)
+        assert rel_err(p, O.density_fp64(O.repack(x, cols), h)) < REL
+        for hv in (1e-6, 50.0):
+            p = c.combined_densities(x, None, cols, [hv] * d)
+            assert rel_err(p, O.density_fp64(O.repack(x, cols), [hv] * d)) < REL
