@@ -310,12 +310,9 @@ def main():
             launches += st.kernel_launches
     barrier()
     wall = time.perf_counter() - wall0
-    ms = statistics.mean(step_ms)
-    if dist is not None:
-        t = torch.tensor([ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = support * ws / (ms / 1e3)
+    from entropical_gb300.replicas import aggregate
+    units, ms = aggregate(support, statistics.mean(step_ms), dist, device=f"cuda:{local}")
+    value = units / (ms / 1e3)
 
     # end to end through the host-buffer call (pinned host input)
     xp = torch.from_numpy(x).pin_memory()

@@ -89,6 +89,7 @@ def main() -> None:
         g["est_negs"] = O.ref_run_mode("negs", est, bw, Path(td) / "ng").ravel()
         g["est_kldiv"] = O.ref_run_mode("kldiv", est, bw, Path(td) / "kl")
         g["est_dens2"] = O.ref_run_mode("dens", est, bw, Path(td) / "d2", dims=2)
+        g["est_dens3"] = O.ref_run_mode("dens", est, bw, Path(td) / "d3", dims=3)
     out = ROOT / "tests" / "golden" / "reference_golden.npz"
     np.savez_compressed(out, **g)
     print("wrote", out, out.stat().st_size, "bytes")

@@ -45,3 +45,8 @@ def test_plain_amise_loop_matches_batched_search(ctx, golden):
         assert calls == 16
         assert np.float32(h) == ref
     assert np.array_equal(hb, golden["hest_amise"])
+
+
+def test_dens_triples(ctx, golden):
+    est = ReferenceEstimators(ctx)
+    assert close(est.dens_nd(golden["est_x"], golden["est_h"], 3), golden["est_dens3"], rtol=1e-4)
