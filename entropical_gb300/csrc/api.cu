@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -356,36 +357,21 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
   InstDev* di = arena_upload(c, hi, &e);
   if (e != cudaSuccess) return c.cuda_fail(e, "upload instances");
 
-  // 4. strip partition (stable, keeps dimension-0 order inside strips)
+  // Every upload and allocation happens before the kernel sequence, which is
+  // captured into one CUDA graph and launched once.
+  uint32_t* dseg_inst = nullptr;
+  uint64_t* dseg_off = nullptr;
+  SegBuild sb;
+  SegTableDev segt{};
   if (!seg_inst.empty()) {
-    uint32_t* dseg_inst = arena_upload(c, seg_inst, &e);
+    dseg_inst = arena_upload(c, seg_inst, &e);
     if (e != cudaSuccess) return c.cuda_fail(e, "upload seg inst");
-    uint64_t* dseg_off = arena_upload(c, seg_off, &e);
+    dseg_off = arena_upload(c, seg_off, &e);
     if (e != cudaSuccess) return c.cuda_fail(e, "upload seg off");
-    e = launch_strip_keys(st, di, dseg_inst, dseg_off, (uint32_t)seg_inst.size(),
-                          max_n, sk, svals);
-    if (e != cudaSuccess) return c.cuda_fail(e, "strip keys");
-    c.stats.kernel_launches += 1;
-    SegBuild sb;
     for (size_t q = 0; q < seg_inst.size(); ++q) sb.add(seg_off[q], hi[seg_inst[q]].n);
-    SegTableDev t;
-    int s = sb.upload(c, &t);
+    int s = sb.upload(c, &segt);
     if (s) return s;
-    uint32_t *k0 = sk, *v0 = svals, *k1 = sk2, *v1 = sv2;
-    e = seg_radix_sort(st, t, (uint32_t)seg_inst.size(), sb.total_blocks, k0, v0,
-                       k1, v1, 0, strip_bits);
-    if (e != cudaSuccess) return c.cuda_fail(e, "strip sort");
-    c.stats.kernel_launches += 3 * (strip_bits / 8);
   }
-
-  // 5. strips, tiles, points, plan
-  e = launch_strip_bounds(st, di, ni, max_n);
-  if (e != cudaSuccess) return c.cuda_fail(e, "strip bounds");
-  e = launch_tile_offsets(st, di, ni);
-  if (e != cudaSuccess) return c.cuda_fail(e, "tile offsets");
-  e = launch_gather_pts(st, di, ni, max_n);
-  if (e != cudaSuccess) return c.cuda_fail(e, "gather points");
-  c.stats.kernel_launches += 3;
   // instance index for every slot: inst_tile_base must be ascending, so the
   // plan kernel searches the instances in slot order.
   std::vector<uint32_t> slot_order(ni);
@@ -406,41 +392,86 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
   uint64_t* dnsrc = static_cast<uint64_t*>(c.arena.alloc(sizeof(uint64_t) * 3));
   double* tile_ls = static_cast<double*>(c.arena.alloc(sizeof(double) * (size_t)n_slots));
   uint32_t* wc = static_cast<uint32_t*>(c.arena.alloc(sizeof(uint32_t) * 4));
-  if (!tiles || !dnsrc || !tile_ls || !wc) return c.fail(ENT_ERR_CUDA, "out of device memory");
-  cudaMemsetAsync(dnsrc, 0, sizeof(uint64_t) * 3, st);
-  e = launch_plan(st, di_sorted, ni, dbase, tiles, n_slots, dnsrc);
-  if (e != cudaSuccess) return c.cuda_fail(e, "plan");
-  c.stats.kernel_launches += 1;
+  double* dls = static_cast<double*>(c.arena.alloc(sizeof(double) * ni));
+  if (!tiles || !dnsrc || !tile_ls || !wc || !dls)
+    return c.fail(ENT_ERR_CUDA, "out of device memory");
 
-  // 6. pair kernel, one persistent launch per dimension present.
-  // The tile descriptors carry indices into the slot-sorted instance array.
-  cudaEventRecord(c.ev_k0, st);
-  for (int d = 1; d <= 3; ++d) {
-    if (group_slots[d] == 0) continue;
-    int launched = 0;
-    cudaEventRecord(c.ev_d[d - 1][0], st);
-    e = launch_density(st, d, c.tile_r[d - 1],
-                       density_variant_supported(d, c.tile_r[d - 1], c.pair_variant)
-                           ? c.pair_variant : 0,
-                       tiles + group_base[d], group_slots[d], di_sorted,
-                       wc + d, c.d_err, tile_ls + group_base[d], mode, c.n_sms,
-                       &launched);
-    if (e != cudaSuccess) return c.cuda_fail(e, "density kernel");
-    cudaEventRecord(c.ev_d[d - 1][1], st);
-    c.ran_d[d - 1] = true;
-    c.stats.kernel_launches += 1;
-  }
-  cudaEventRecord(c.ev_k1, st);
-  if (mode & (DM_LOGSUM | DM_SUMV)) {
-    double* dls = static_cast<double*>(c.arena.alloc(sizeof(double) * ni));
-    if (!dls) return c.fail(ENT_ERR_CUDA, "out of device memory");
-    e = launch_inst_logsum(st, di_sorted, ni, tile_ls, dls);
-    if (e != cudaSuccess) return c.cuda_fail(e, "instance log-sum");
-    c.stats.kernel_launches += 1;
-    if (out) {
-      out->d_logsum_sorted = dls;
-      out->slot_order = slot_order;
+  const bool graph = c.use_graphs;
+  auto rec = [&](cudaEvent_t ev) {
+    return graph ? cudaEventRecordWithFlags(ev, st, cudaEventRecordExternal)
+                 : cudaEventRecord(ev, st);
+  };
+  uint32_t launches = 0;
+  auto sequence = [&]() -> cudaError_t {
+    cudaError_t r;
+    // 4. strip partition (stable, keeps dimension-0 order inside strips)
+    if (!seg_inst.empty()) {
+      r = launch_strip_keys(st, di, dseg_inst, dseg_off, (uint32_t)seg_inst.size(), max_n, sk,
+                            svals);
+      if (r != cudaSuccess) return r;
+      uint32_t *k0 = sk, *v0 = svals, *k1 = sk2, *v1 = sv2;
+      r = seg_radix_sort(st, segt, (uint32_t)seg_inst.size(), sb.total_blocks, k0, v0, k1, v1,
+                         0, strip_bits);
+      if (r != cudaSuccess) return r;
+      launches += 1 + 3 * (strip_bits / 8);
     }
+    // 5. strips, tiles, points, plan
+    if ((r = launch_strip_bounds(st, di, ni, max_n)) != cudaSuccess) return r;
+    if ((r = launch_tile_offsets(st, di, ni)) != cudaSuccess) return r;
+    if ((r = launch_gather_pts(st, di, ni, max_n)) != cudaSuccess) return r;
+    if ((r = cudaMemsetAsync(dnsrc, 0, sizeof(uint64_t) * 3, st)) != cudaSuccess) return r;
+    if ((r = launch_plan(st, di_sorted, ni, dbase, tiles, n_slots, dnsrc)) != cudaSuccess) return r;
+    launches += 4;
+    // 6. pair kernel, one persistent launch per dimension present; the tile
+    // descriptors carry indices into the slot-sorted instance array
+    rec(c.ev_k0);
+    for (int d = 1; d <= 3; ++d) {
+      if (group_slots[d] == 0) continue;
+      int launched = 0;
+      rec(c.ev_d[d - 1][0]);
+      r = launch_density(st, d, c.tile_r[d - 1],
+                         density_variant_supported(d, c.tile_r[d - 1], c.pair_variant[d - 1])
+                             ? c.pair_variant[d - 1] : 0,
+                         tiles + group_base[d], group_slots[d], di_sorted, wc + d, c.d_err,
+                         tile_ls + group_base[d], mode, c.n_sms, &launched);
+      if (r != cudaSuccess) return r;
+      rec(c.ev_d[d - 1][1]);
+      c.ran_d[d - 1] = true;
+      launches += 1;
+    }
+    rec(c.ev_k1);
+    if (mode & (DM_LOGSUM | DM_SUMV)) {
+      if ((r = launch_inst_logsum(st, di_sorted, ni, tile_ls, dls)) != cudaSuccess) return r;
+      launches += 1;
+    }
+    return cudaSuccess;
+  };
+  if (graph) {
+    e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return c.cuda_fail(e, "begin capture");
+    cudaError_t es = sequence();
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(st, &g);
+    if (es != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return c.cuda_fail(es, "batch kernels");
+    }
+    if (e != cudaSuccess) return c.cuda_fail(e, "end capture");
+    cudaGraphExec_t ge = nullptr;
+    e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return c.cuda_fail(e, "graph instantiate");
+    e = cudaGraphLaunch(ge, st);
+    cudaGraphExecDestroy(ge);
+    if (e != cudaSuccess) return c.cuda_fail(e, "graph launch");
+  } else {
+    e = sequence();
+    if (e != cudaSuccess) return c.cuda_fail(e, "batch kernels");
+  }
+  c.stats.kernel_launches += launches;
+  if ((mode & (DM_LOGSUM | DM_SUMV)) && out) {
+    out->d_logsum_sorted = dls;
+    out->slot_order = slot_order;
   }
   e = cudaMemcpyAsync(c.h_nsrc_d, dnsrc, sizeof(uint64_t) * 3, cudaMemcpyDeviceToHost, st);
   if (e != cudaSuccess) return c.cuda_fail(e, "read pair count");
@@ -514,6 +545,7 @@ int ent_create(ent_ctx** out, int device) {
     delete c;
     return ENT_ERR_CUDA;
   }
+  if (const char* g = std::getenv("ENT_NO_GRAPHS")) c->use_graphs = (g[0] == '0');
   *out = reinterpret_cast<ent_ctx*>(c);
   return ENT_OK;
 }
@@ -561,8 +593,9 @@ int ent_set_tuning(ent_ctx* ctx, const ent_tuning* t) {
     if (t->targets_per_warp[d - 1] && !density_r_supported(d, (int)t->targets_per_warp[d - 1]))
       return c->fail(ENT_ERR_ARG, "unsupported targets_per_warp");
   if (t->cells_per_h > 4) return c->fail(ENT_ERR_ARG, "cells_per_h must be 1..4");
-  if (t->pair_variant > 2) return c->fail(ENT_ERR_ARG, "pair_variant must be 0..2");
-  if (t->pair_variant) c->pair_variant = (int)t->pair_variant - 1;
+  if (t->pair_variant > 4) return c->fail(ENT_ERR_ARG, "pair_variant must be 0..4");
+  if (t->pair_variant)
+    for (int d = 0; d < 3; ++d) c->pair_variant[d] = (int)t->pair_variant - 1;
   for (int d = 1; d <= 3; ++d)
     if (t->targets_per_warp[d - 1]) c->tile_r[d - 1] = (int)t->targets_per_warp[d - 1];
   if (t->cells_per_h) c->strip_subdiv = t->cells_per_h;
@@ -574,7 +607,7 @@ int ent_get_tuning(const ent_ctx* ctx, ent_tuning* t) {
   const Ctx* c = reinterpret_cast<const Ctx*>(ctx);
   for (int d = 0; d < 3; ++d) t->targets_per_warp[d] = (uint32_t)c->tile_r[d];
   t->cells_per_h = c->strip_subdiv;
-  t->pair_variant = (uint32_t)c->pair_variant + 1;
+  t->pair_variant = (uint32_t)c->pair_variant[1] + 1;
   return ENT_OK;
 }
 

@@ -40,7 +40,10 @@ struct Ctx {
   bool pending_pairs = false;
   uint32_t strip_subdiv = 2;  // cells per bandwidth along dimension 1 (d = 2)
   int tile_r[3] = {16, 16, 8};  // targets per warp of the pair kernel, by d
-  int pair_variant = 1;         // pair body: 0 min-based, 1 saturating FMA (faster)
+  // pair body per dimension: 0 min-based, 1 saturating FMA, 2 saturating at
+  // 5 CTAs/SM, 3 as 2 with larger chunks (fastest measured: 2, 2, 1)
+  int pair_variant[3] = {2, 2, 1};
+  bool use_graphs = true;       // capture the batch kernel sequence in a CUDA graph
 
   // grid of a persistent kernel: resident CTAs per SM x SMs, capped by work
   unsigned persistent_grid(uint32_t n_work, const void* kern, int threads, size_t smem);

@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(128)
     const float* __restrict__ xs = Cc.xs;
     const uint32_t nch = (nsrc + CC::CH - 1) / CC::CH;
     if (tid == 0 && nch > 0)
-      issue_chunk<1, R>(0, q & 1u, nsrc, nr, run_lo, run_pre, xs, bufs, ptab, npc, full);
+      issue_chunk<CC>(0, q & 1u, nsrc, nr, run_lo, run_pre, xs, bufs, ptab, npc, full);
     float coef[2];
 #pragma unroll
     for (int k = 0; k < 2; ++k) coef[k] = -2.25f / st[s_col].piv[k];
@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(128)
     for (uint32_t c = 0; c < nch; ++c) {
       const uint32_t qq = q + c, b = qq & 1u;
       if (tid == 0 && c + 1 < nch)
-        issue_chunk<1, R>(c + 1, (qq + 1) & 1u, nsrc, nr, run_lo, run_pre, xs, bufs, ptab,
+        issue_chunk<CC>(c + 1, (qq + 1) & 1u, nsrc, nr, run_lo, run_pre, xs, bufs, ptab,
                           npc, full);
       const bool ok = mbar_wait(&full[b], (qq >> 1) & 1u);
       if (ok) {

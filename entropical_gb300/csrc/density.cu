@@ -319,12 +319,28 @@ __global__ void k_plan(const InstDev* __restrict__ insts, uint32_t n_inst,
 }
 
 // ------------------------------------------------------- pair kernel
+// Pair-body variants V: 0 min-based; 1 saturating FMA; 2 saturating FMA at
+// 5 resident CTAs per SM; 3 as 2 with 1.5x larger staged chunks.
+template <int V>
+struct VariantTraits {
+  static constexpr int MINB = V >= 2 ? 5 : 1;
+  static constexpr int CHX_D1 = V == 3 ? 6144 : 0;
+  static constexpr int CHX_D2 = V == 3 ? 3072 : 0;
+  static constexpr int CHX_D3 = V == 3 ? 1536 : 0;
+};
+
+template <int D, int V>
+__host__ __device__ constexpr int chunk_of() {
+  return D == 1 ? VariantTraits<V>::CHX_D1
+                : (D == 2 ? VariantTraits<V>::CHX_D2 : VariantTraits<V>::CHX_D3);
+}
+
 template <int D, int R, int V>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, VariantTraits<V>::MINB)
     k_density(const TileDesc* __restrict__ tiles, uint32_t n_slots,
               const InstDev* __restrict__ insts, uint32_t* work_counter,
               uint32_t* err, double* tile_logsum, uint32_t mode) {
-  typedef Cfg<D, R> C;
+  typedef Cfg<D, R, chunk_of<D, V>()> C;
   typedef typename C::P P;
   extern __shared__ __align__(128) unsigned char dsm[];
   P* bufs = reinterpret_cast<P*>(dsm);
@@ -379,8 +395,7 @@ __global__ void __launch_bounds__(128)
     const f32x2 M1 = (D == 1) ? pk2(ng0, ng0) : pk2(ng0, ng1);
     const uint32_t nch = (nsrc + C::CH - 1) / C::CH;
     if (tid == 0 && nch > 0)
-      issue_chunk<D, R>(0, q & 1u, nsrc, nr, run_lo, run_pre, pts, bufs, ptab,
-                        npc, full);
+      issue_chunk<C>(0, q & 1u, nsrc, nr, run_lo, run_pre, pts, bufs, ptab, npc, full);
 
     // Register-resident targets of this warp; missing ones sit far away.
     float ks[R], kc[R];
@@ -419,8 +434,8 @@ __global__ void __launch_bounds__(128)
     for (uint32_t c = 0; c < nch; ++c) {
       const uint32_t qq = q + c, b = qq & 1u;
       if (tid == 0 && c + 1 < nch)
-        issue_chunk<D, R>(c + 1, (qq + 1) & 1u, nsrc, nr, run_lo, run_pre, pts,
-                          bufs, ptab, npc, full);
+        issue_chunk<C>(c + 1, (qq + 1) & 1u, nsrc, nr, run_lo, run_pre, pts, bufs, ptab,
+                       npc, full);
       const bool ok = mbar_wait(&full[b], (qq >> 1) & 1u);
       if (ok) {
         const P* B = bufs + (size_t)b * C::CAP;
@@ -455,7 +470,7 @@ __global__ void __launch_bounds__(128)
             }
 #pragma unroll
             for (int r = 0; r < R; ++r) kahan_add(ks[r], kc[r], acc[r]);
-          } else if constexpr (V == 1) {
+          } else if constexpr (V >= 1) {
             // saturating body: (g^2 - d^2)^+ = sat(fma(-d, d, g^2)) because
             // g^2 < 1; all work on the FMA pipe, no min on the ALU
             const float g2a = -ng0, g2b = -ng1, g2c = -ng2;
@@ -639,7 +654,7 @@ cudaError_t launch_density_t(cudaStream_t st, const TileDesc* tiles,
                              uint32_t* work_counter, uint32_t* err,
                              double* tile_logsum, uint32_t mode, int n_sms,
                              int* launched) {
-  typedef Cfg<D, R> C;
+  typedef Cfg<D, R, chunk_of<D, V>()> C;
   auto kern = k_density<D, R, V>;
   cudaError_t e = cudaFuncSetAttribute(
       kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM);
@@ -686,7 +701,7 @@ __global__ void __launch_bounds__(256)
 // Targets per warp: the tunable variants of each dimension (tile = 4 warps).
 int density_variant_supported(int d, int r, int v) {
   if (v == 0) return density_r_supported(d, r);
-  return v == 1 && r == (d == 3 ? 8 : 16);
+  return v >= 1 && v <= 3 && r == (d == 3 ? 8 : 16);
 }
 
 int density_r_supported(int d, int r) {
@@ -772,12 +787,18 @@ cudaError_t launch_density(cudaStream_t st, int d, int r, int v, const TileDesc*
   ENT_LAUNCH(1, 8, 0)
   ENT_LAUNCH(1, 16, 0)
   ENT_LAUNCH(1, 16, 1)
+  ENT_LAUNCH(1, 16, 2)
+  ENT_LAUNCH(1, 16, 3)
   ENT_LAUNCH(2, 8, 0)
   ENT_LAUNCH(2, 16, 0)
   ENT_LAUNCH(2, 16, 1)
+  ENT_LAUNCH(2, 16, 2)
+  ENT_LAUNCH(2, 16, 3)
   ENT_LAUNCH(3, 4, 0)
   ENT_LAUNCH(3, 8, 0)
   ENT_LAUNCH(3, 8, 1)
+  ENT_LAUNCH(3, 8, 2)
+  ENT_LAUNCH(3, 8, 3)
 #undef ENT_LAUNCH
   return cudaErrorInvalidValue;
 }

@@ -16,7 +16,8 @@ template <> struct PtType<1> { typedef float T; };
 template <> struct PtType<2> { typedef float2 T; };
 template <> struct PtType<3> { typedef float4 T; };
 
-template <int D, int R>
+// CHX: elements per staged chunk (0 = default for the dimension)
+template <int D, int R, int CHX = 0>
 struct Cfg {
   static constexpr int NW = 4;
   static constexpr int NT = NW * 32;
@@ -24,7 +25,7 @@ struct Cfg {
   typedef typename PtType<D>::T P;
   static constexpr int E = sizeof(P);
   static constexpr int A = 16 / E;  // 16-byte alignment, in elements
-  static constexpr int CH = (D == 1) ? 4096 : (D == 2 ? 2048 : 1024);
+  static constexpr int CH = CHX ? CHX : ((D == 1) ? 4096 : (D == 2 ? 2048 : 1024));
   static constexpr int MAXP = MAX_RUNS + 1;
   static constexpr int CAP = CH + 2 * A * MAXP;
   static constexpr size_t SMEM = 2 * (size_t)CAP * E;
@@ -38,13 +39,11 @@ struct Piece {
   uint32_t o;    // shared-memory element offset of the copy
 };
 
-template <int D, int R>
+template <class C>
 __device__ __forceinline__ void issue_chunk(
     uint32_t c, uint32_t b, uint32_t nsrc, uint32_t nr, const uint32_t* run_lo,
-    const uint32_t* run_pre, const typename Cfg<D, R>::P* pts,
-    typename Cfg<D, R>::P* bufs, Piece (*ptab)[Cfg<D, R>::MAXP], uint32_t* npc,
-    uint64_t* full) {
-  typedef Cfg<D, R> C;
+    const uint32_t* run_pre, const typename C::P* pts, typename C::P* bufs,
+    Piece (*ptab)[C::MAXP], uint32_t* npc, uint64_t* full) {
   const uint32_t begin = c * C::CH;
   const uint32_t end = min(begin + (uint32_t)C::CH, nsrc);
   uint32_t np = 0, o = 0, bytes = 0;

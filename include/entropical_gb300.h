@@ -65,8 +65,12 @@ typedef struct {
   uint32_t targets_per_warp[3]; /* per density dimension: d=1,2: 8 or 16;
                                    d=3: 4 or 8 (tile = 4 warps) */
   uint32_t cells_per_h;         /* d=2 strips: cells per bandwidth, 1..4 */
-  uint32_t pair_variant;        /* pair body + 1: 1 = min-based (packed
-                                   sub/fma, 2 min), 2 = saturating FMA */
+  uint32_t pair_variant;        /* pair body + 1, for every dimension:
+                                   1 = min-based (packed sub/fma, 2 min),
+                                   2 = saturating FMA, 3 = saturating at 5
+                                   CTAs/SM, 4 = as 3 with 1.5x larger chunks;
+                                   default per dimension: 3, 3, 2 (get
+                                   reports dimension 2) */
 } ent_tuning;
 
 /* Context lifecycle. device < 0 selects the current device. */

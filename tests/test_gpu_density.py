@@ -178,7 +178,7 @@ def test_mi_config_pair_sampled(ctx):
     assert rel_err(p[t], f) < REL
 
 
-@pytest.mark.parametrize("variant", [0, 1])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
 @pytest.mark.parametrize("d", [1, 2, 3])
 def test_pair_body_variants(d, variant):
     from entropical_gb300 import Context
