@@ -75,8 +75,10 @@ def tune(ctx: Context, run, d: int, n: int, repeats: int = 2, save: bool = True)
     for (r, s, v) in CANDIDATES[d]:
         tpw = list(before["targets_per_warp"])
         tpw[d - 1] = r
-        ctx.set_tuning(tpw, s, v)
-        run()  # warm-up (also compiles nothing: all variants are prebuilt)
+        pv = [None, None, None]
+        pv[d - 1] = v
+        ctx.set_tuning(tpw, s, pv)
+        run()  # warm-up (all variants are prebuilt)
         best = math.inf
         for _ in range(repeats):
             run()
@@ -85,7 +87,9 @@ def tune(ctx: Context, run, d: int, n: int, repeats: int = 2, save: bool = True)
     best, r, s, v = min(results)
     tpw = list(before["targets_per_warp"])
     tpw[d - 1] = r
-    ctx.set_tuning(tpw, s, v)
+    pv = [None, None, None]
+    pv[d - 1] = v
+    ctx.set_tuning(tpw, s, pv)
     choice = {"targets_per_warp": r, "cells_per_h": s, "pair_variant": v, "ms": best,
               "all": [{"r": rr, "s": ss, "v": vv, "ms": mm} for mm, rr, ss, vv in results]}
     if save:
@@ -102,5 +106,7 @@ def apply(ctx: Context, d: int, n: int) -> bool:
         return False
     tpw = list(ctx.tuning()["targets_per_warp"])
     tpw[d - 1] = c["targets_per_warp"]
-    ctx.set_tuning(tpw, c["cells_per_h"], c["pair_variant"])
+    pv = [None, None, None]
+    pv[d - 1] = c["pair_variant"]
+    ctx.set_tuning(tpw, c["cells_per_h"], pv)
     return True

@@ -594,8 +594,12 @@ int ent_set_tuning(ent_ctx* ctx, const ent_tuning* t) {
       return c->fail(ENT_ERR_ARG, "unsupported targets_per_warp");
   if (t->cells_per_h > 4) return c->fail(ENT_ERR_ARG, "cells_per_h must be 1..4");
   if (t->pair_variant > 4) return c->fail(ENT_ERR_ARG, "pair_variant must be 0..4");
+  for (int d = 0; d < 3; ++d)
+    if (t->pair_variant_by_dim[d] > 4) return c->fail(ENT_ERR_ARG, "pair_variant must be 0..4");
   if (t->pair_variant)
     for (int d = 0; d < 3; ++d) c->pair_variant[d] = (int)t->pair_variant - 1;
+  for (int d = 0; d < 3; ++d)
+    if (t->pair_variant_by_dim[d]) c->pair_variant[d] = (int)t->pair_variant_by_dim[d] - 1;
   for (int d = 1; d <= 3; ++d)
     if (t->targets_per_warp[d - 1]) c->tile_r[d - 1] = (int)t->targets_per_warp[d - 1];
   if (t->cells_per_h) c->strip_subdiv = t->cells_per_h;
@@ -608,6 +612,7 @@ int ent_get_tuning(const ent_ctx* ctx, ent_tuning* t) {
   for (int d = 0; d < 3; ++d) t->targets_per_warp[d] = (uint32_t)c->tile_r[d];
   t->cells_per_h = c->strip_subdiv;
   t->pair_variant = (uint32_t)c->pair_variant[1] + 1;
+  for (int d = 0; d < 3; ++d) t->pair_variant_by_dim[d] = (uint32_t)c->pair_variant[d] + 1;
   return ENT_OK;
 }
 

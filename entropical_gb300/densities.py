@@ -99,17 +99,23 @@ class Context:
         t = _native.Tuning()
         self.check(self._lib.ent_get_tuning(self._h, C.byref(t)))
         return {"targets_per_warp": list(t.targets_per_warp), "cells_per_h": t.cells_per_h,
-                "pair_variant": t.pair_variant - 1}
+                "pair_variant": t.pair_variant - 1,
+                "pair_variant_by_dim": [v - 1 for v in t.pair_variant_by_dim]}
 
     def set_tuning(self, targets_per_warp=(0, 0, 0), cells_per_h: int = 0,
                    pair_variant: int | None = None) -> None:
         """Tile shapes and pair body (0 min-based, 1 saturating FMA, 2 the same at
-        5 CTAs/SM, 3 as 2 with larger chunks); 0/None keeps."""
+        5 CTAs/SM, 3 as 2 with larger chunks) for every dimension, or a list of
+        three per-dimension bodies; 0/None keeps."""
         t = _native.Tuning()
         for i, v in enumerate(targets_per_warp):
             t.targets_per_warp[i] = int(v)
         t.cells_per_h = int(cells_per_h)
-        t.pair_variant = 0 if pair_variant is None else int(pair_variant) + 1
+        if isinstance(pair_variant, (list, tuple)):
+            for i, v in enumerate(pair_variant):
+                t.pair_variant_by_dim[i] = 0 if v is None else int(v) + 1
+        else:
+            t.pair_variant = 0 if pair_variant is None else int(pair_variant) + 1
         self.check(self._lib.ent_set_tuning(self._h, C.byref(t)))
 
     def _selection(self, i_cols, h, tau):

@@ -71,6 +71,8 @@ typedef struct {
                                    CTAs/SM, 4 = as 3 with 1.5x larger chunks;
                                    default per dimension: 3, 3, 2 (get
                                    reports dimension 2) */
+  uint32_t pair_variant_by_dim[3]; /* the same per dimension (0 = keep);
+                                      applied after pair_variant */
 } ent_tuning;
 
 /* Context lifecycle. device < 0 selects the current device. */
