@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-compare", action="store_true",
                     help="skip the batched+learned vs plain comparison")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the supplementary measurements of the other configurations")
     ap.add_argument("--coords", type=int, default=N_COORDS,
                     help="coordinates of the MI batch (64 = the benchmark workload; "
                          "smaller values give the small case used for ncu captures)")
@@ -220,6 +222,48 @@ def compare_plain(ctx, x, ptr, log_fp64_pairs=2):
     return out
 
 
+def other_configs(ctx):
+    """The other configurations, measured once (device time of one call each):
+    config 1 (1-D GMM density), config 3 (TE, all ordered pairs, 3 lags) and
+    config 4 (512 uneven instances: one batch vs sequential plain calls)."""
+    from entropical_gb300 import workloads
+    out = {}
+    x1 = workloads.gmm_1d(20_000, seed=42)[None]
+    ctx.combined_densities(x1, None, [0], [0.1])
+    ctx.combined_densities(x1, None, [0], [0.1])
+    st = ctx.last_stats()
+    sup = float(ctx.support_counts(x1, None, [0], [0.1]).sum())
+    out["gmm1d_20k"] = {"ms": st.total_ms, "support_pairs": sup,
+                        "pairs_per_s": sup / (st.total_ms / 1e3)}
+    xt, _ = workloads.langevin(32, 200_000, seed=11)
+    ht = workloads.scott_bandwidth(xt, 3)
+    taus = [1, 5, 10]
+    te = ctx.te_all_pairs(xt, ht, taus)
+    st = ctx.last_stats()
+    cnt = ctx.te_all_pairs(xt, ht, taus, counts=True)
+    sup3 = float(cnt.sum() - sum(np.trace(c) for c in cnt))
+    out["te_32x200k_3lags"] = {
+        "ms": st.total_ms, "densities": st.instances, "te_estimates": 3 * 32 * 31,
+        "te_estimates_per_s": 3 * 32 * 31 / (st.total_ms / 1e3),
+        "pair_kernel_ms_by_dim": list(st.pair_kernel_ms_by_dim),
+        "support_pairs_3d": sup3, "candidate_pairs_3d": st.candidate_pairs_by_dim[2],
+        "h2d_bytes": int(xt.nbytes)}
+    ub = workloads.uneven_batch(512, seed=5)
+    H = ctx.entropy_batch(ub)
+    H = ctx.entropy_batch(ub)
+    st = ctx.last_stats()
+    supu = float(ctx.entropy_batch(ub, counts=True).sum())
+    t0 = time.perf_counter()
+    for xq, hq in ub:
+        ctx.combined_densities(xq, None, list(range(xq.shape[0])), hq)
+    seq = time.perf_counter() - t0
+    out["uneven_512"] = {"batched_ms": st.total_ms, "sequential_plain_s": seq,
+                         "speedup": seq / (st.total_ms / 1e3), "support_pairs": supu,
+                         "pairs_per_s": supu / (st.total_ms / 1e3),
+                         "points": int(sum(xq.shape[1] for xq, _ in ub))}
+    return out
+
+
 def reference_arm(args, x, h):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -355,7 +399,7 @@ def main():
         "gpu_launches": launches,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": traffic,
-                     "kernel": "k_density<2,16> (2-D pair kernel)",
+                     "kernel": "k_density<2,16,2> (2-D pair kernel)",
                      "flops_per_pair": 10, "peak_kind": peak_note},
     }
     if not args.no_compare and ws == 1:
@@ -363,6 +407,11 @@ def main():
             line["batched_learned_vs_plain"] = compare_plain(ctx, x, ptr)
         except Exception as exc:
             line["batched_learned_vs_plain"] = {"error": str(exc)[:300]}
+    if not args.no_extra and ws == 1:
+        try:
+            line["other_configs"] = other_configs(ctx)
+        except Exception as exc:
+            line["other_configs"] = {"error": str(exc)[:300]}
     if not args.no_cpu_baseline and ws == 1:
         try:
             from oracle import oracle as O
