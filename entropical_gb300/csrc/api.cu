@@ -258,6 +258,17 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
   uint32_t slot = 0;
   uint32_t max_n = 0;
   uint32_t max_strips = 1;
+  // pair body per dimension; the symmetric body has no counting mode
+  int var_d[4] = {0, 0, 0, 0};
+  bool sym_d[4] = {false, false, false, false};
+  for (int d = 1; d <= 3; ++d) {
+    int v = c.pair_variant[d - 1];
+    if (!density_variant_supported(d, c.tile_r[d - 1], v)) v = 0;
+    if (pair_is_sym(v) && (mode & DM_COUNT)) v = 2;
+    var_d[d] = v;
+    sym_d[d] = pair_is_sym(v);
+  }
+  uint64_t sym_points = 0;
   for (int d = 1; d <= 3; ++d) {
     group_base[d] = slot;
     for (uint32_t i : order) {
@@ -307,12 +318,15 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
       }
       I.n_strips = I.ncell1 * I.ncell2;
       max_strips = std::max(max_strips, I.n_strips);
-      I.tt = (uint32_t)density_tile_targets((int)s.d, c.tile_r[s.d - 1]);
+      I.tt = (uint32_t)density_tile_targets(
+          (int)s.d, sym_d[d] ? sym_tile_r(d, var_d[d]) : c.tile_r[s.d - 1]);
       I.tile_cap = (s.n + I.tt - 1) / I.tt + std::min(I.n_strips, s.n);
       I.tile_base = slot;
       slot += I.tile_cap;
       I.scale = (mode & DM_COUNT) ? 1.0 : std::pow(0.75, (double)s.d) / (s.norm * prod_hg2);
       I.out = s.out;
+      I.sym = sym_d[d] ? 1u : 0u;
+      if (I.sym) sym_points += s.n;
     }
     group_slots[d] = slot - group_base[d];
   }
@@ -337,6 +351,18 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
       seg_off.push_back(seg_tot);
       seg_tot += I.n;
     }
+  }
+  // FP64 sums of the symmetric instances, one block zeroed in the sequence
+  double* sym_acc = nullptr;
+  if (sym_points) {
+    sym_acc = static_cast<double*>(c.arena.alloc(sizeof(double) * sym_points));
+    if (!sym_acc) return c.fail(ENT_ERR_CUDA, "out of device memory");
+    uint64_t o = 0;
+    for (uint32_t i = 0; i < ni; ++i)
+      if (hi[i].sym) {
+        hi[i].acc = sym_acc + o;
+        o += hi[i].n;
+      }
   }
   uint32_t *sk = nullptr, *svals = nullptr, *sk2 = nullptr, *sv2 = nullptr;
   int strip_bits = bits_for(max_strips);
@@ -420,6 +446,9 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
     if ((r = launch_tile_offsets(st, di, ni)) != cudaSuccess) return r;
     if ((r = launch_gather_pts(st, di, ni, max_n)) != cudaSuccess) return r;
     if ((r = cudaMemsetAsync(dnsrc, 0, sizeof(uint64_t) * 3, st)) != cudaSuccess) return r;
+    if (sym_acc &&
+        (r = cudaMemsetAsync(sym_acc, 0, sizeof(double) * sym_points, st)) != cudaSuccess)
+      return r;
     if ((r = launch_plan(st, di_sorted, ni, dbase, tiles, n_slots, dnsrc)) != cudaSuccess) return r;
     launches += 4;
     // 6. pair kernel, one persistent launch per dimension present; the tile
@@ -429,15 +458,19 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
       if (group_slots[d] == 0) continue;
       int launched = 0;
       rec(c.ev_d[d - 1][0]);
-      r = launch_density(st, d, c.tile_r[d - 1],
-                         density_variant_supported(d, c.tile_r[d - 1], c.pair_variant[d - 1])
-                             ? c.pair_variant[d - 1] : 0,
-                         tiles + group_base[d], group_slots[d], di_sorted, wc + d, c.d_err,
-                         tile_ls + group_base[d], mode, c.n_sms, &launched);
+      r = launch_density(st, d, c.tile_r[d - 1], var_d[d], tiles + group_base[d],
+                         group_slots[d], di_sorted, wc + d, c.d_err, tile_ls + group_base[d],
+                         mode, c.n_sms, &launched);
       if (r != cudaSuccess) return r;
       rec(c.ev_d[d - 1][1]);
       c.ran_d[d - 1] = true;
       launches += 1;
+      if (sym_d[d]) {
+        r = launch_sym_finish(st, tiles + group_base[d], group_slots[d], di_sorted,
+                              tile_ls + group_base[d], mode);
+        if (r != cudaSuccess) return r;
+        launches += 1;
+      }
     }
     rec(c.ev_k1);
     if (mode & (DM_LOGSUM | DM_SUMV)) {
@@ -593,9 +626,10 @@ int ent_set_tuning(ent_ctx* ctx, const ent_tuning* t) {
     if (t->targets_per_warp[d - 1] && !density_r_supported(d, (int)t->targets_per_warp[d - 1]))
       return c->fail(ENT_ERR_ARG, "unsupported targets_per_warp");
   if (t->cells_per_h > 4) return c->fail(ENT_ERR_ARG, "cells_per_h must be 1..4");
-  if (t->pair_variant > 4) return c->fail(ENT_ERR_ARG, "pair_variant must be 0..4");
+  if (t->pair_variant > PAIR_SYM + 2) return c->fail(ENT_ERR_ARG, "pair_variant must be 0..6");
   for (int d = 0; d < 3; ++d)
-    if (t->pair_variant_by_dim[d] > 4) return c->fail(ENT_ERR_ARG, "pair_variant must be 0..4");
+    if (t->pair_variant_by_dim[d] > PAIR_SYM + 2)
+      return c->fail(ENT_ERR_ARG, "pair_variant must be 0..6");
   if (t->pair_variant)
     for (int d = 0; d < 3; ++d) c->pair_variant[d] = (int)t->pair_variant - 1;
   for (int d = 0; d < 3; ++d)

@@ -42,7 +42,7 @@ struct Ctx {
   int tile_r[3] = {16, 16, 8};  // targets per warp of the pair kernel, by d
   // pair body per dimension: 0 min-based, 1 saturating FMA, 2 saturating at
   // 5 CTAs/SM, 3 as 2 with larger chunks (fastest measured: 2, 2, 1)
-  int pair_variant[3] = {2, 2, 1};
+  int pair_variant[3] = {4, 4, 4};  // PAIR_SYM (engine.h): symmetric bodies
   bool use_graphs = true;       // capture the batch kernel sequence in a CUDA graph
 
   // grid of a persistent kernel: resident CTAs per SM x SMs, capped by work

@@ -130,6 +130,20 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
 
 // Orderable 32-bit key of a float: unsigned compare == float compare
 // (-0.0 sorts just before +0.0; NaN never reaches here).
+// float -> double by re-biasing the IEEE-754 fields on the integer pipes
+// (exact for normal floats; zero and subnormals give 0). The FP64 pipe of
+// this GPU runs at a small fraction of the FP32 rate, so conversions on the
+// hot path avoid it. Inputs must be finite.
+__device__ __forceinline__ double f32_to_f64_int(float v) {
+  const uint32_t b = __float_as_uint(v);
+  const uint32_t e = (b >> 23) & 0xffu;
+  if (e == 0) return 0.0;
+  const uint64_t r = ((uint64_t)(b & 0x80000000u) << 32) |
+                     ((uint64_t)(e + (1023u - 127u)) << 52) |
+                     ((uint64_t)(b & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)r);
+}
+
 __device__ __forceinline__ uint32_t float_key(float f) {
   uint32_t u = __float_as_uint(f);
   return (u & 0x80000000u) ? ~u : (u | 0x80000000u);

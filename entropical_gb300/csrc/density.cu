@@ -288,7 +288,11 @@ __global__ void k_plan(const InstDev* __restrict__ insts, uint32_t n_inst,
   auto add_strip = [&](uint32_t sp) {
     const uint32_t a0 = I.strip_start[sp], b0 = I.strip_start[sp + 1];
     if (a0 == b0) return;
-    const uint32_t l = lower_y(I.pts, d, a0, b0, vlo);
+    // symmetric mode: sources before the tile's first target are skipped
+    // (their tiles evaluate those pairs)
+    if (I.sym && b0 <= tb) return;
+    uint32_t l = lower_y(I.pts, d, a0, b0, vlo);
+    if (I.sym) l = max(l, tb);
     const uint32_t h = upper_y(I.pts, d, l, b0, vhi);
     if (h <= l) return;
     if (nr > 0 && td.lo[nr - 1] + td.len[nr - 1] == l) {
@@ -320,7 +324,9 @@ __global__ void k_plan(const InstDev* __restrict__ insts, uint32_t n_inst,
 
 // ------------------------------------------------------- pair kernel
 // Pair-body variants V: 0 min-based; 1 saturating FMA; 2 saturating FMA at
-// 5 resident CTAs per SM; 3 as 2 with 1.5x larger staged chunks.
+// 5 resident CTAs per SM; 3 as 2 with 1.5x larger staged chunks. (The
+// symmetric bodies PAIR_SYM and PAIR_SYM + 1 are k_density_sym,
+// density_sym.cu.)
 template <int V>
 struct VariantTraits {
   static constexpr int MINB = V >= 2 ? 5 : 1;
@@ -701,6 +707,7 @@ __global__ void __launch_bounds__(256)
 // Targets per warp: the tunable variants of each dimension (tile = 4 warps).
 int density_variant_supported(int d, int r, int v) {
   if (v == 0) return density_r_supported(d, r);
+  if (pair_is_sym(v)) return d >= 1 && d <= 3;  // own tile shape, sym_tile_r
   return v >= 1 && v <= 3 && r == (d == 3 ? 8 : 16);
 }
 
@@ -780,6 +787,9 @@ cudaError_t launch_density(cudaStream_t st, int d, int r, int v, const TileDesc*
                            uint32_t* work_counter, uint32_t* err,
                            double* tile_logsum, uint32_t mode, int n_sms,
                            int* launched) {
+  if (pair_is_sym(v))
+    return launch_density_sym(st, d, v, tiles, n_slots, insts, work_counter, err, n_sms,
+                              launched);
 #define ENT_LAUNCH(D, R, V)                                                         \
   if (d == D && r == R && v == V)                                                   \
     return launch_density_t<D, R, V>(st, tiles, n_slots, insts, work_counter, err,  \

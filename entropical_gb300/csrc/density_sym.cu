@@ -1,0 +1,342 @@
+// Symmetric pair kernel: every unordered (target, source) pair inside the
+// candidate runs is evaluated once and added to both points.
+//
+// The reference sums, for every target i, K(x_i - x_k) over all k
+// (densities_omp.cpp:67-159, density_2d.cuh:34-100); the product kernel is
+// symmetric, K(x_i - x_k) == K(x_k - x_i) bit for bit (x_i - x_k is the exact
+// negation of x_k - x_i), so each pair can serve both sums. The tile plan
+// (k_plan with InstDev::sym) keeps, for a tile of targets [tb, tb + tc) in
+// strip-major order, only the sources at positions >= tb:
+//   * sources in [tb, tb + tc) (the tile itself) are evaluated in both orders
+//     and added on the target side only;
+//   * sources at >= tb + tc are added to the target (registers) and to the
+//     source: each warp stores its per-source sum over its R targets in its
+//     own shared-memory row (one float per staged element); once per chunk
+//     the four rows are added in a fixed order and flushed into the FP64
+//     sums InstDev::acc, so the FP32 part of every sum is deterministic;
+//   * a source before tb belongs to an earlier tile, which evaluates the pair.
+// Target-side sums are flushed into the same FP64 array once per chunk (warp
+// transpose-sum, one FP64 atomic per target), so no per-target compensation
+// state is carried and a warp can hold 32 targets. k_sym_finish scales the
+// sums and writes densities or per-tile log-sums.
+//
+// Every mbarrier wait is bounded; on expiry the kernel reports EF_TIMEOUT,
+// waits (bounded) for its own copies in flight and returns.
+#include "staging.cuh"
+
+namespace ent {
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+// Staged elements per chunk; shared memory per CTA = chunk buffers x 2 plus
+// one float row per warp (4 x CAP floats): 51 KB (d = 1, 2) and 38 KB (d = 3),
+// so that 4 resp. 5 CTAs fit an SM.
+template <int D>
+struct SymChunk {
+  static constexpr int CH = D == 1 ? 2048 : (D == 2 ? 1536 : 768);
+};
+
+template <int D, int R, int MINB>
+__global__ void __launch_bounds__(128, MINB)
+    k_density_sym(const TileDesc* __restrict__ tiles, uint32_t n_slots,
+                  const InstDev* __restrict__ insts, uint32_t* work_counter,
+                  uint32_t* err) {
+  typedef Cfg<D, R, SymChunk<D>::CH> C;
+  typedef typename C::P P;
+  static_assert(R <= 32 && (R & (R - 1)) == 0, "R: power of two <= 32");
+  extern __shared__ __align__(128) unsigned char dsm[];
+  P* bufs = reinterpret_cast<P*>(dsm);
+  float* srow = reinterpret_cast<float*>(dsm + C::SMEM);  // C::NW rows of CAP floats
+  __shared__ __align__(8) uint64_t full[2];
+  __shared__ Piece ptab[2][C::MAXP];
+  __shared__ uint32_t npc[2];
+  __shared__ uint32_t run_lo[MAX_RUNS], run_pre[MAX_RUNS + 1];
+  __shared__ uint32_t s_g, s_nr, s_tb, s_tc, s_inst;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) {
+    mbar_init(&full[0], 1);
+    mbar_init(&full[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  float* myrow = srow + (size_t)warp * C::CAP;
+  uint32_t q = 0;
+
+  for (;;) {
+    if (tid == 0) {
+      const uint32_t g = atomicAdd(work_counter, 1u);
+      s_g = g;
+      if (g < n_slots) {
+        const TileDesc* T = tiles + g;
+        const uint32_t nr = T->n_runs;
+        s_tb = T->t_begin;
+        s_tc = T->t_count;
+        s_inst = T->inst;
+        s_nr = nr;
+        run_pre[0] = 0;
+        for (uint32_t r = 0; r < nr; ++r) {
+          run_lo[r] = T->lo[r];
+          run_pre[r + 1] = run_pre[r] + T->len[r];
+        }
+      }
+    }
+    __syncthreads();
+    const uint32_t g = s_g;
+    if (g >= n_slots) break;
+    const uint32_t tc = s_tc;
+    if (tc == 0) {
+      __syncthreads();
+      continue;
+    }
+    const InstDev* I = insts + s_inst;
+    const P* __restrict__ pts = reinterpret_cast<const P*>(I->pts);
+    double* __restrict__ acc64 = I->acc;
+    const uint32_t nr = s_nr, nsrc = run_pre[nr], tb = s_tb, tend = tb + tc;
+    const float g2a = I->g2[0], g2b = I->g2[D > 1 ? 1 : 0], g2c = I->g2[D > 2 ? 2 : 0];
+    const uint32_t nch = (nsrc + C::CH - 1) / C::CH;
+    if (tid == 0 && nch > 0)
+      issue_chunk<C>(0, q & 1u, nsrc, nr, run_lo, run_pre, pts, bufs, ptab, npc, full);
+
+    // Register-resident targets of this warp; missing ones sit at +inf, where
+    // every term is 0.
+    const float FAR = __int_as_float(0x7f800000);
+    f32x2 T01[D == 1 ? 1 : R];
+    float T2[D == 2 ? 1 : R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const uint32_t li = warp * R + r;
+      P p;
+      if (li < tc) {
+        p = pts[tb + li];
+      } else {
+        if constexpr (D == 1) p = FAR;
+        else if constexpr (D == 2) p = make_float2(FAR, FAR);
+        else p = make_float4(FAR, FAR, FAR, 0.f);
+      }
+      if constexpr (D == 1) {
+        T2[r] = p;
+      } else if constexpr (D == 2) {
+        T01[r] = pk2(p.x, p.y);
+      } else {
+        T01[r] = pk2(p.x, p.y);
+        T2[r] = p.z;
+      }
+    }
+    const int tgt = lane >> (5 - Log2<R>::v);
+    const bool writer = (lane & ((32 / R) - 1)) == 0;
+    const uint32_t my_li = warp * R + tgt;
+
+    bool aborted = false;
+    uint32_t ab_q = 0;
+    bool ab_next = false;
+    for (uint32_t c = 0; c < nch; ++c) {
+      const uint32_t qq = q + c, b = qq & 1u;
+      if (tid == 0 && c + 1 < nch)
+        issue_chunk<C>(c + 1, (qq + 1) & 1u, nsrc, nr, run_lo, run_pre, pts, bufs, ptab,
+                       npc, full);
+      const bool ok = mbar_wait(&full[b], (qq >> 1) & 1u);
+      float acc[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) acc[r] = 0.f;
+      if (ok) {
+        const P* B = bufs + (size_t)b * C::CAP;
+        const uint32_t np = npc[b];
+        for (uint32_t pi = 0; pi < np; ++pi) {
+          const uint32_t s0 = ptab[b][pi].s0, n = ptab[b][pi].n;
+          if constexpr (D == 1) {
+            f32x2 accp[R / 2];
+            f32x2 T[R / 2];
+#pragma unroll
+            for (int i = 0; i < R / 2; ++i) {
+              accp[i] = pk2(0.f, 0.f);
+              T[i] = pk2(T2[2 * i], T2[2 * i + 1]);
+            }
+#pragma unroll 2
+            for (uint32_t k = lane; k < n; k += 32) {
+              const float s = B[s0 + k];
+              const f32x2 S = pk2(s, s);
+              f32x2 src0 = pk2(0.f, 0.f), src1 = pk2(0.f, 0.f);
+#pragma unroll
+              for (int i = 0; i < R / 2; ++i) {
+                float da, db;
+                upk2(sub2(T[i], S), da, db);
+                const f32x2 w = pk2(__saturatef(__fmaf_rn(-da, da, g2a)),
+                                    __saturatef(__fmaf_rn(-db, db, g2a)));
+                accp[i] = add2(accp[i], w);
+                if (i & 1) src1 = add2(src1, w);
+                else src0 = add2(src0, w);
+              }
+              float u0, u1, u2, u3;
+              upk2(src0, u0, u1);
+              upk2(src1, u2, u3);
+              myrow[s0 + k] = (u0 + u1) + (u2 + u3);
+            }
+#pragma unroll
+            for (int i = 0; i < R / 2; ++i) {
+              float a0, a1;
+              upk2(accp[i], a0, a1);
+              acc[2 * i] += a0;
+              acc[2 * i + 1] += a1;
+            }
+          } else {
+#pragma unroll 2
+            for (uint32_t k = lane; k < n; k += 32) {
+              const P s = B[s0 + k];
+              const f32x2 S = pk2(s.x, s.y);
+              // source-side sum over the warp's R targets in 4 interleaved
+              // partials (short rounding and dependency chains)
+              float src[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+              for (int r = 0; r < R; ++r) {
+                float dx, dy;
+                upk2(sub2(T01[r], S), dx, dy);
+                const float wx = __saturatef(__fmaf_rn(-dx, dx, g2a));
+                const float wy = __saturatef(__fmaf_rn(-dy, dy, g2b));
+                if constexpr (D == 2) {
+                  acc[r] = __fmaf_rn(wx, wy, acc[r]);
+                  src[r & 3] = __fmaf_rn(wx, wy, src[r & 3]);
+                } else {
+                  const float dz = T2[r] - s.z;
+                  const float wz = __saturatef(__fmaf_rn(-dz, dz, g2c));
+                  const float wxy = wx * wy;
+                  acc[r] = __fmaf_rn(wxy, wz, acc[r]);
+                  src[r & 3] = __fmaf_rn(wxy, wz, src[r & 3]);
+                }
+              }
+              myrow[s0 + k] = (src[0] + src[1]) + (src[2] + src[3]);
+            }
+          }
+        }
+      }
+      if (__syncthreads_or(!ok)) {
+        aborted = true;
+        ab_q = qq;
+        ab_next = c + 1 < nch;
+        break;
+      }
+      // Target side of this chunk: lanes combined, one FP64 add per target.
+      const float tot = warp_transpose_sum<R>(acc, lane);
+      if (writer && my_li < tc && tot != 0.f)
+        atomicAdd(acc64 + tb + my_li, f32_to_f64_int(tot));
+      // Source side: every warp wrote every staged element of this chunk
+      // into its row; the tile's own targets are complete on the target side.
+      const uint32_t np = npc[b];
+      for (uint32_t pi = 0; pi < np; ++pi) {
+        const Piece p = ptab[b][pi];
+        const uint32_t a = p.g0 + (p.s0 - p.o);
+        for (uint32_t k = tid; k < p.n; k += C::NT) {
+          if (a + k < tend) continue;
+          const uint32_t e = p.s0 + k;
+          const float v = (srow[e] + srow[C::CAP + e]) + (srow[2 * C::CAP + e] + srow[3 * C::CAP + e]);
+          if (v != 0.f) atomicAdd(acc64 + a + k, f32_to_f64_int(v));
+        }
+      }
+      __syncthreads();
+    }
+    if (aborted) {
+      if (tid == 0) {
+        atomicOr(err, EF_TIMEOUT);
+        mbar_wait(&full[ab_q & 1u], (ab_q >> 1) & 1u);
+        if (ab_next) mbar_wait(&full[(ab_q + 1) & 1u], ((ab_q + 1) >> 1) & 1u);
+      }
+      __syncthreads();
+      return;
+    }
+    q += nch;
+  }
+}
+
+template <int D, int R, int MINB>
+cudaError_t launch_sym_t(cudaStream_t st, const TileDesc* tiles, uint32_t n_slots,
+                         const InstDev* insts, uint32_t* work_counter, uint32_t* err,
+                         int n_sms, int* launched) {
+  typedef Cfg<D, R, SymChunk<D>::CH> C;
+  auto kern = k_density_sym<D, R, MINB>;
+  static_assert(C::NW == 4, "four warp rows");
+  const size_t smem = C::SMEM + (size_t)C::NW * C::CAP * sizeof(float);
+  cudaError_t e =
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, C::NT, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  uint64_t grid = (uint64_t)per_sm * (uint64_t)n_sms;
+  if (grid > n_slots) grid = n_slots;
+  if (grid == 0) grid = 1;
+  e = cudaMemsetAsync(work_counter, 0, sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
+  kern<<<(unsigned)grid, C::NT, smem, st>>>(tiles, n_slots, insts, work_counter, err);
+  if (launched) *launched = (int)grid;
+  return cudaGetLastError();
+}
+
+// Symmetric epilogue: one warp per tile slot turns the FP64 sums of its
+// targets into densities (scale), written by original index and/or summed
+// (log or value) into the slot's tile_logsum.
+__global__ void __launch_bounds__(256)
+    k_sym_finish(const TileDesc* __restrict__ tiles, uint32_t n_slots,
+                 const InstDev* __restrict__ insts, double* tile_logsum,
+                 uint32_t mode) {
+  const uint32_t g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (g >= n_slots) return;  // warp-uniform
+  const TileDesc& T = tiles[g];
+  const uint32_t tc = T.t_count;
+  double ls = 0.0;
+  if (tc) {
+    const InstDev& I = insts[T.inst];
+    for (uint32_t li = lane; li < tc; li += 32) {
+      const uint32_t k = T.t_begin + li;
+      const double dens = I.scale * I.acc[k];
+      if (mode & DM_WRITE_F64) I.out[I.perm[k]] = dens;
+      if (mode & DM_LOGSUM) ls += log(dens);
+      else if (mode & DM_SUMV) ls += dens;
+    }
+  }
+  if (mode & (DM_LOGSUM | DM_SUMV)) {
+    for (int o = 16; o; o >>= 1) ls += __shfl_xor_sync(FULL, ls, o);
+    if (lane == 0) tile_logsum[g] = ls;
+  }
+}
+
+}  // namespace
+
+// Targets per warp of the symmetric bodies: PAIR_SYM 32 (d = 1, 2; 4 CTAs
+// per SM) / 16 (d = 3; 5 CTAs per SM); PAIR_SYM + 1 16 / 8 at 5 CTAs per SM.
+int sym_tile_r(int d, int v) {
+  if (v == PAIR_SYM) return d == 3 ? 16 : 32;
+  return d == 3 ? 8 : 16;
+}
+
+cudaError_t launch_density_sym(cudaStream_t st, int d, int v, const TileDesc* tiles,
+                               uint32_t n_slots, const InstDev* insts,
+                               uint32_t* work_counter, uint32_t* err, int n_sms,
+                               int* launched) {
+  const int r = sym_tile_r(d, v);
+#define ENT_SYM(D, R, M)                                                               \
+  if (d == D && r == R)                                                                \
+    return launch_sym_t<D, R, M>(st, tiles, n_slots, insts, work_counter, err, n_sms, \
+                                 launched);
+  ENT_SYM(1, 32, 4)
+  ENT_SYM(1, 16, 5)
+  ENT_SYM(2, 32, 4)
+  ENT_SYM(2, 16, 5)
+  ENT_SYM(3, 16, 5)
+  ENT_SYM(3, 8, 5)
+#undef ENT_SYM
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_sym_finish(cudaStream_t st, const TileDesc* tiles,
+                              uint32_t n_slots, const InstDev* insts,
+                              double* tile_logsum, uint32_t mode) {
+  if (n_slots == 0) return cudaSuccess;
+  const uint64_t blocks = ((uint64_t)n_slots * 32 + 255) / 256;
+  k_sym_finish<<<(unsigned)blocks, 256, 0, st>>>(tiles, n_slots, insts, tile_logsum, mode);
+  return cudaGetLastError();
+}
+
+}  // namespace ent

@@ -63,7 +63,8 @@ struct InstDev {
   double scale;             // 0.75^d / (norm * prod h_j * prod g_j^2)
   double* out;              // per-point density by original index (nullable)
   uint32_t tt;              // targets per tile
-  uint32_t pad;
+  uint32_t sym;             // 1: symmetric evaluation (each unordered pair once)
+  double* acc;              // symmetric mode: unscaled sums by sorted position
 };
 
 struct TileDesc {
@@ -102,7 +103,8 @@ cudaError_t launch_gather_pts(cudaStream_t st, const InstDev* insts,
 cudaError_t launch_plan(cudaStream_t st, const InstDev* insts, uint32_t n_inst,
                         const uint32_t* inst_tile_base, TileDesc* tiles,
                         uint32_t n_slots, uint64_t* n_src_total);
-// v: pair body, 0 = min-based, 1 = saturating FMA (needs g^2 < 1)
+// v: pair body, 0 = min-based, 1 = saturating FMA (needs g^2 < 1), 2-3 as 1
+// with other occupancy / chunk sizes, 4-5 symmetric (PAIR_SYM; r ignored)
 cudaError_t launch_density(cudaStream_t st, int d, int r, int v, const TileDesc* tiles,
                            uint32_t n_slots, const InstDev* insts,
                            uint32_t* work_counter, uint32_t* err,
@@ -118,6 +120,23 @@ cudaError_t launch_density(cudaStream_t st, int d, int r, const TileDesc* tiles,
 int density_r_supported(int d, int r);
 int density_variant_supported(int d, int r, int v);
 int density_tile_targets(int d, int r);
+// Pair bodies PAIR_SYM and PAIR_SYM + 1 (density_sym.cu) evaluate every
+// unordered pair once and add it to both points: the plan keeps only sources
+// at or after the tile's first target (InstDev::sym), the kernel accumulates
+// into InstDev::acc (zeroed first), and launch_sym_finish turns the sums
+// into the epilogue of `mode`. Their tile shape is their own (sym_tile_r).
+constexpr int PAIR_SYM = 4;
+__host__ __device__ constexpr bool pair_is_sym(int v) {
+  return v == PAIR_SYM || v == PAIR_SYM + 1;
+}
+int sym_tile_r(int d, int v);
+cudaError_t launch_density_sym(cudaStream_t st, int d, int v, const TileDesc* tiles,
+                               uint32_t n_slots, const InstDev* insts,
+                               uint32_t* work_counter, uint32_t* err, int n_sms,
+                               int* launched_ctas);
+cudaError_t launch_sym_finish(cudaStream_t st, const TileDesc* tiles,
+                              uint32_t n_slots, const InstDev* insts,
+                              double* tile_logsum, uint32_t mode);
 cudaError_t launch_inst_logsum(cudaStream_t st, const InstDev* insts,
                                uint32_t n_inst, const double* tile_logsum,
                                double* inst_logsum);

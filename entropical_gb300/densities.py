@@ -105,8 +105,9 @@ class Context:
     def set_tuning(self, targets_per_warp=(0, 0, 0), cells_per_h: int = 0,
                    pair_variant: int | None = None) -> None:
         """Tile shapes and pair body (0 min-based, 1 saturating FMA, 2 the same at
-        5 CTAs/SM, 3 as 2 with larger chunks) for every dimension, or a list of
-        three per-dimension bodies; 0/None keeps."""
+        5 CTAs/SM, 3 as 2 with larger chunks, 4 symmetric at 5 CTAs/SM, 5
+        symmetric at 4 CTAs/SM) for every dimension, or a list of three
+        per-dimension bodies; 0/None keeps."""
         t = _native.Tuning()
         for i, v in enumerate(targets_per_warp):
             t.targets_per_warp[i] = int(v)

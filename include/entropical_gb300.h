@@ -68,9 +68,13 @@ typedef struct {
   uint32_t pair_variant;        /* pair body + 1, for every dimension:
                                    1 = min-based (packed sub/fma, 2 min),
                                    2 = saturating FMA, 3 = saturating at 5
-                                   CTAs/SM, 4 = as 3 with 1.5x larger chunks;
-                                   default per dimension: 3, 3, 2 (get
-                                   reports dimension 2) */
+                                   CTAs/SM, 4 = as 3 with 1.5x larger chunks,
+                                   5 = symmetric (each unordered pair once,
+                                   added to both points; support counts use
+                                   3 instead; own tiles of 128/128/64
+                                   targets), 6 = as 5 with tiles of
+                                   64/64/32 targets; default 5 for every
+                                   dimension (get reports dimension 2) */
   uint32_t pair_variant_by_dim[3]; /* the same per dimension (0 = keep);
                                       applied after pair_variant */
 } ent_tuning;
