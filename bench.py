@@ -408,7 +408,9 @@ def main():
         "gpu_launches": launches,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": traffic,
-                     "kernel": f"k_density<2,16,{var2}> (2-D pair kernel)",
+                     "kernel": (f"k_density_sym<2,{32 if var2 == 4 else 16}> (2-D symmetric "
+                                "pair kernel)" if var2 in (4, 5) else
+                                f"k_density<2,16,{var2}> (2-D pair kernel)"),
                      "flops_per_pair": fpp, "peak_kind": peak_note},
     }
     if not args.no_compare and ws == 1:
