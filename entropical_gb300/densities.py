@@ -21,6 +21,8 @@ COMPAT_NORM = 1
 BATCH_SUPPORT_COUNTS = 2
 BATCH_DEVICE_INPUT = 4
 HEST_THUMB, HEST_AMISE, HEST_AMISE_WARM = 0, 1, 2
+BATCH_DEVICE_OUTPUT = 8
+REF_MI, REF_TRANSS, REF_AUTOENT, REF_NEGS, REF_KLDIV = 1, 2, 3, 4, 5
 
 
 def as_colmajor(coords, n_rows: int | None = None) -> tuple[np.ndarray, int, int]:
@@ -261,6 +263,47 @@ class Context:
         self.check(st)
         return out
 
+    def reference_estimator(self, coords, h: Sequence[float], estimator: int,
+                            tau: int = 0) -> np.ndarray:
+        """One of the reference's estimators (REF_MI, REF_TRANSS, REF_AUTOENT,
+        REF_NEGS, REF_KLDIV) over all columns of coords (n_cols, n_rows) with
+        its own formula, as one device batch (ent_reference_estimator).
+        Returns an (n_cols, n_cols) matrix or an (n_cols,) vector."""
+        flat, n_rows, n_cols = as_colmajor(coords)
+        hv = _f32(h)
+        if len(hv) != n_cols:
+            raise ValueError("one bandwidth per column")
+        vec = estimator in (REF_AUTOENT, REF_NEGS)
+        out = np.zeros(n_cols if vec else n_cols * n_cols, dtype=np.float64)
+        st = self._lib.ent_reference_estimator(
+            self._h, flat.ctypes.data_as(C.c_void_p), n_rows, n_cols,
+            hv.ctypes.data_as(c_f32_p), int(estimator), int(tau), 0,
+            out.ctypes.data_as(c_f64_p))
+        self.check(st)
+        return out if vec else out.reshape(n_cols, n_cols)
+
+    def dens_all(self, coords, h: Sequence[float], dims: int, taus=None) -> np.ndarray:
+        """Sum-normalised densities of every column (dims=1), pair (2) or
+        triple (3) in the reference's order (dens.cpp:19-106), one device
+        batch (ent_dens_all); returns an (n_densities, n_sel) array."""
+        flat, n_rows, n_cols = as_colmajor(coords)
+        hv = _f32(h)
+        if len(hv) != n_cols:
+            raise ValueError("one bandwidth per column")
+        tv = None if taus is None else _u32(taus)
+        if tv is not None and len(tv) != dims:
+            raise ValueError("one lag per density dimension")
+        M = n_cols
+        n_inst = M if dims == 1 else (M * (M - 1) // 2 if dims == 2 else M * (M - 1) * (M - 2) // 6)
+        mx = 0 if (tv is None or dims == 1) else int(tv.max())
+        out = np.zeros((max(n_inst, 1), max(n_rows - mx, 0)), dtype=np.float64)
+        ni, ns = C.c_size_t(), C.c_size_t()
+        st = self._lib.ent_dens_all(
+            self._h, flat.ctypes.data_as(C.c_void_p), n_rows, n_cols, hv.ctypes.data_as(c_f32_p),
+            int(dims), None if tv is None else tv.ctypes.data_as(c_u32_p), 0,
+            out.ctypes.data_as(C.c_void_p), C.byref(ni), C.byref(ns))
+        self.check(st)
+        return out[: ni.value, : ns.value]
 
     # ---------------------------------------------------- neighbour search
     def neighbor_windows(self, col, h: float) -> tuple[np.ndarray, np.ndarray]:

@@ -9,12 +9,18 @@ host with the same formulas, including the float log of tools.cpp:18-37, the
 Kahan normalisation of tools.hxx:33-43 and the Y->X weight of transs.cpp:96.
 They give the reference's numbers; the batched, resubstitution estimators
 are Context.mi_all_pairs / te_all_pairs / entropy_batch.
+
+By default (batched=True) each estimator is one device batch through
+ent_reference_estimator / ent_dens_all (all densities in one engine batch,
+FP64 sums on the device); batched=False keeps the reference's loop structure,
+one density call per density and the sums on the host.
 """
 from __future__ import annotations
 
 import numpy as np
 
-from .densities import Context, as_colmajor
+from .densities import (REF_AUTOENT, REF_KLDIV, REF_MI, REF_NEGS, REF_TRANSS, Context,
+                        as_colmajor)
 
 
 def _flog(x):
@@ -51,14 +57,17 @@ def _inv(x):
 class ReferenceEstimators:
     """The reference's estimators (compat formulas) on a Context."""
 
-    def __init__(self, ctx: Context):
+    def __init__(self, ctx: Context, batched: bool = True):
         self.ctx = ctx
+        self.batched = batched
 
     def _dens(self, x, cols, h, tau=None):
         return self.ctx.combined_densities(x, None, cols, h, tau, compat_norm=True)
 
     def mi(self, coords, h):
         """Mi::main (mi.cpp:37-59): sum_k p_ij log(p_ij / p_i / p_j), float accumulator."""
+        if self.batched:
+            return self.ctx.reference_estimator(coords, h, REF_MI).astype(np.float32)
         x, n_rows, n = as_colmajor(coords)
         x = x.reshape(n, n_rows)
         out = np.zeros((n, n), np.float32)
@@ -73,6 +82,8 @@ class ReferenceEstimators:
 
     def transs(self, coords, h, tau: int):
         """Transs::main (transs.cpp:39-115), including the reference's weights."""
+        if self.batched:
+            return self.ctx.reference_estimator(coords, h, REF_TRANSS, tau)
         x, n_rows, n = as_colmajor(coords)
         x = x.reshape(n, n_rows)
         p = [self._dens(x, [i], [h[i]]) for i in range(n)]
@@ -96,6 +107,8 @@ class ReferenceEstimators:
 
     def autoent(self, coords, h, tau: int):
         """AutoEnt::main (autoent.cpp:39-58)."""
+        if self.batched:
+            return self.ctx.reference_estimator(coords, h, REF_AUTOENT, tau)
         x, n_rows, n = as_colmajor(coords)
         x = x.reshape(n, n_rows)
         out = np.zeros(n, np.float64)
@@ -110,6 +123,8 @@ class ReferenceEstimators:
 
     def negs(self, coords, h):
         """Negs::main (negs.cpp:36-47): -sum_k p log p of the sum-normalised density."""
+        if self.batched:
+            return self.ctx.reference_estimator(coords, h, REF_NEGS).astype(np.float32)
         x, n_rows, n = as_colmajor(coords)
         x = x.reshape(n, n_rows)
         out = np.zeros(n, np.float32)
@@ -120,6 +135,8 @@ class ReferenceEstimators:
 
     def kldiv(self, coords, h):
         """KLDiv::main (kldiv.cpp:36-54)."""
+        if self.batched:
+            return self.ctx.reference_estimator(coords, h, REF_KLDIV)
         x, n_rows, n = as_colmajor(coords)
         x = x.reshape(n, n_rows)
         ps = [sum1_normalized(self._dens(x, [i], [h[i]])) for i in range(n)]
@@ -130,10 +147,21 @@ class ReferenceEstimators:
                 out[j, i] = np.sum(ps[j] * _flog(ps[j] / ps[i]))
         return out
 
+    def dens_1d(self, coords, h):
+        """Dens::compute_densities_1d (dens.cpp:19-47): sum-normalised density of
+        every column, concatenated."""
+        if self.batched:
+            return self.ctx.dens_all(coords, h, 1).reshape(-1)
+        x, n_rows, n = as_colmajor(coords)
+        x = x.reshape(n, n_rows)
+        return np.concatenate([sum1_normalized(self._dens(x, [i], [h[i]])) for i in range(n)])
+
     def dens_nd(self, coords, h, dims: int, taus=None):
         """Dens::compute_densities_nd (dens.cpp:49-106): sum-normalised densities of
         all column pairs (dims=2) or triples (dims=3), concatenated in the
         reference's order."""
+        if self.batched:
+            return self.ctx.dens_all(coords, h, dims, taus).reshape(-1)
         x, n_rows, n = as_colmajor(coords)
         x = x.reshape(n, n_rows)
         taus = [0] * dims if taus is None else list(taus)

@@ -192,6 +192,54 @@ typedef struct {
 int ent_entropy_batch(ent_ctx* ctx, const ent_instance* inst, size_t n_inst,
                       uint32_t flags, double* h_out);
 
+/* ------------------------------------ the reference's estimator formulas */
+
+#define ENT_BATCH_DEVICE_OUTPUT 8u /* ent_dens_all: out is a device pointer */
+
+#define ENT_REF_MI 1u      /* Mi::main, mi.cpp:37-59 */
+#define ENT_REF_TRANSS 2u  /* Transs::main, transs.cpp:39-115 */
+#define ENT_REF_AUTOENT 3u /* AutoEnt::main, autoent.cpp:39-58 */
+#define ENT_REF_NEGS 4u    /* Negs::main, negs.cpp:36-47 */
+#define ENT_REF_KLDIV 5u   /* KLDiv::main, kldiv.cpp:36-54 */
+
+/*
+ * One of the reference's estimators over all columns, with the reference's
+ * own formula (not the resubstitution estimators above), as ONE batch: every
+ * density it needs is an instance of one engine batch (marginals once), the
+ * per-point densities stay in device memory and the sums run on the device in
+ * FP64. Densities are normalised by n_rows as the reference's CUDA build does
+ * (densities_cuda.cu:98-103); logs are the reference's float log, 0 at 0
+ * (tools.cpp:18-37). Replaces the estimator main loops and their per-density
+ * combined_densities() calls. out (host):
+ *   ENT_REF_MI      n_cols x n_cols, out[i][j] = sum_k p_ij log(p_ij/p_i/p_j),
+ *                   symmetric, zero diagonal
+ *   ENT_REF_TRANSS  n_cols x n_cols, lag tau: out[i][j] (i < j) the
+ *                   p(x_i, x_i+tau, x_j) term with weight h_i h_i h_j, out[j][i]
+ *                   the p(x_i, x_j, x_j+tau) term with weight h_i h_j h_i, as
+ *                   transs.cpp:75-104 (non-finite terms and p > 1 skipped)
+ *   ENT_REF_AUTOENT n_cols, lag tau
+ *   ENT_REF_NEGS    n_cols, -sum_k p~ log p~ with p~ = p / sum(p)
+ *   ENT_REF_KLDIV   n_cols x n_cols, out[i][j] = sum_k p~_i log(p~_i / p~_j)
+ * flags: ENT_BATCH_DEVICE_INPUT for device coordinates. No counterpart of
+ * this batched form exists in the reference (its mains loop on the host).
+ */
+int ent_reference_estimator(ent_ctx* ctx, const float* coords, size_t n_rows,
+                            size_t n_cols, const float* h, uint32_t estimator,
+                            uint32_t tau, uint32_t flags, double* out);
+
+/*
+ * Dens::compute_densities_1d / _nd (dens.cpp:19-106) as ONE batch: the
+ * sum-normalised densities of every column (dims = 1), every column pair
+ * (dims = 2) or triple (dims = 3, the "dens -D 3" mode) in the reference's
+ * order (i < j < k), each over lags taus[0..dims) (NULL: none; ignored for
+ * dims = 1). out: *n_inst rows of *n_sel = n_rows - max(taus) values, host
+ * memory, or device memory with ENT_BATCH_DEVICE_OUTPUT. At most 65535
+ * densities per call.
+ */
+int ent_dens_all(ent_ctx* ctx, const float* coords, size_t n_rows, size_t n_cols,
+                 const float* h, uint32_t dims, const uint32_t* taus,
+                 uint32_t flags, double* out, size_t* n_inst, size_t* n_sel);
+
 /* ---------------------------------------------------- neighbour search */
 
 #define ENT_NB_WINDOW 0u /* reference boxes() windows (densities_omp.cpp:33-65) */

@@ -196,6 +196,104 @@ def te_fp64(x: np.ndarray, y: np.ndarray, tau: int, hx: float, hy: float) -> flo
     return float(np.mean(l3 + l1 - l2a - l2b))
 
 
+def _flog32(v):
+    """Tools::select_log(false) (tools.cpp:18-37): float log of the value cast
+    to float, 0 at 0."""
+    v32 = np.asarray(v, dtype=np.float64).astype(np.float32)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return np.where(v32 == 0, np.float32(0), np.log(v32)).astype(np.float64)
+
+
+def _inv(v):
+    v = np.asarray(v, dtype=np.float64)
+    with np.errstate(divide="ignore"):
+        return np.where(v == 0, v, 1.0 / v)
+
+
+def reference_estimator_fp64(x: np.ndarray, h, estimator: str, tau: int = 0,
+                             bound: bool = False):
+    """The reference estimators' formulas (mi.cpp:37-59, transs.cpp:39-115,
+    autoent.cpp:39-58, negs.cpp:36-47, kldiv.cpp:36-54) over FP64 oracle
+    densities normalised by n_rows (densities_cuda.cu:98-103), with the float
+    log of tools.cpp:18-37 and FP64 sums. x: (n_cols, n_rows).
+
+    bound=True also returns, per output, sum_k (|term_k| + |weight_k|) (weight
+    = the factor in front of the log): the scale against which float-log
+    results are compared (a relative density error e moves a term by at most
+    e (|term| + 3 |weight|), a float rounding of the log argument by 6e-8
+    |weight|)."""
+    x = np.asarray(x, np.float32)
+    M, N = x.shape
+    h = np.asarray(h, np.float32)
+    bnd = None
+
+    def dens(cols, lags=None):
+        lags = [0] * len(cols) if lags is None else lags
+        n = N - max(lags)
+        sel = np.stack([x[c][l:l + n] for c, l in zip(cols, lags)])
+        return density_fp64(sel, [h[c] for c in cols], norm=float(N))
+
+    if estimator == "mi":
+        p = [dens([i]) for i in range(M)]
+        out, bnd = np.zeros((M, M)), np.zeros((M, M))
+        for i in range(M):
+            for j in range(i + 1, M):
+                pij = dens([i, j])
+                t = pij * _flog32(pij / p[i] / p[j])
+                out[i, j] = out[j, i] = np.sum(t)
+                bnd[i, j] = bnd[j, i] = np.sum(np.abs(t) + np.abs(pij))
+        return (out, bnd) if bound else out
+    if estimator == "transs":
+        m = N - tau
+        p = [dens([i]) for i in range(M)]
+        pt = [dens([i, i], [0, tau]) for i in range(M)]
+        out, bnd = np.zeros((M, M)), np.zeros((M, M))
+        for i in range(M):
+            for j in range(i + 1, M):
+                hi, hj = float(h[i]), float(h[j])
+                pij = dens([i, j])
+                for (a, b, p3, w, pp, ptt) in (
+                        (i, j, dens([i, i, j], [0, tau, 0]), (hi, hi, hj), p[i], pt[i]),
+                        (j, i, dens([i, j, j], [0, 0, tau]), (hi, hj, hi), p[j], pt[j])):
+                    p3, pp, pq, ptt = p3[:m], pp[:m], pij[:m], ptt[:m]
+                    arg = p3 * pp * _inv(pq) * _inv(ptt)
+                    with np.errstate(invalid="ignore"):
+                        te = p3 * w[0] * w[1] * w[2] * _flog32(arg)
+                    ok = (p3 > 0) & np.isfinite(te) & (p3 <= 1.0)
+                    out[a, b] = np.sum(te[ok])
+                    bnd[a, b] = np.sum(np.abs(te[ok]) + np.abs(p3 * w[0] * w[1] * w[2])[ok])
+        return (out, bnd) if bound else out
+    if estimator == "autoent":
+        out, bnd = np.zeros(M), np.zeros(M)
+        for i in range(M):
+            hh = float(h[i])
+            p1 = dens([i], [tau])
+            p2 = dens([i, i], [0, tau])
+            ok = p2 > 0
+            t = (p2 * hh * hh * _flog32(p1 * _inv(p2 * hh)))[ok]
+            out[i] = np.sum(t)
+            bnd[i] = np.sum(np.abs(t) + (p2 * hh * hh)[ok])
+        return (out, bnd) if bound else out
+    ps = []
+    for i in range(M):
+        p = dens([i])
+        ps.append(p / p.sum())
+    if estimator == "negs":
+        out = np.array([-np.sum(_flog32(q) * q) for q in ps])
+        bnd = np.array([np.sum(np.abs(_flog32(q) * q) + q) for q in ps])
+        return (out, bnd) if bound else out
+    if estimator == "kldiv":
+        out, bnd = np.zeros((M, M)), np.zeros((M, M))
+        for i in range(M):
+            for j in range(M):
+                if i != j:
+                    t = ps[i] * _flog32(ps[i] / ps[j])
+                    out[i, j] = np.sum(t)
+                    bnd[i, j] = np.sum(np.abs(t) + ps[i])
+        return (out, bnd) if bound else out
+    raise ValueError(estimator)
+
+
 # ------------------------------------------------------- reference build
 def ref_densities(coords: np.ndarray, cols, h, tau=None) -> np.ndarray:
     """The reference's OpenMP combined_densities on repacked columns (float32,

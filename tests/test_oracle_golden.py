@@ -82,3 +82,14 @@ def test_live_reference_boxes_ties():
     lo, hi = O.ref_boxes(col, 0.1)
     lo2, hi2 = O.boxes(col, 0.1)
     assert np.array_equal(lo, lo2) and np.array_equal(hi, hi2)
+
+
+@pytest.mark.parametrize("name,key,tau", [("mi", "est_mi", 0), ("transs", "est_transs", 2),
+                                          ("autoent", "est_autoent", 2), ("negs", "est_negs", 0),
+                                          ("kldiv", "est_kldiv", 0)])
+def test_reference_estimator_formulas_vs_golden(golden, name, key, tau):
+    """The FP64 restatement of the reference estimator formulas reproduces the
+    reference's own estimator outputs (printed to 6 significant digits)."""
+    r = O.reference_estimator_fp64(golden["est_x"], golden["est_h"], name, tau)
+    g = golden[key].reshape(r.shape)
+    assert np.allclose(r, g, rtol=2e-5, atol=1e-6)
