@@ -264,6 +264,22 @@ def other_configs(ctx):
                          "speedup": seq / (st.total_ms / 1e3), "support_pairs": supu,
                          "pairs_per_s": supu / (st.total_ms / 1e3),
                          "points": int(sum(xq.shape[1] for xq, _ in ub))}
+    # the reference's own estimator formulas, one device batch each
+    from entropical_gb300.densities import REF_MI, REF_TRANSS
+    xm = workloads.mi_coords(100_000, 64, seed=2024)
+    hm = workloads.scott_bandwidth(xm, 2)
+    ref = {}
+    for name, xx, hh, kind, tau in (("mi_64x100k", xm, hm, REF_MI, 0),
+                                    ("transs_32x200k_tau5", xt, ht, REF_TRANSS, 5)):
+        ctx.reference_estimator(xx, hh, kind, tau)
+        st = ctx.last_stats()
+        ref[name] = {"ms": st.total_ms, "densities": st.instances,
+                     "pair_kernel_ms_by_dim": list(st.pair_kernel_ms_by_dim)}
+    d3 = ctx.dens_all(xm[:16], hm[:16], 3)
+    st = ctx.last_stats()
+    ref["dens_D3_16x100k"] = {"ms": st.total_ms, "densities": int(d3.shape[0]),
+                              "d2h_bytes": int(d3.nbytes)}
+    out["reference_formulas"] = ref
     return out
 
 
