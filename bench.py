@@ -280,6 +280,29 @@ def other_configs(ctx):
     ref["dens_D3_16x100k"] = {"ms": st.total_ms, "densities": int(d3.shape[0]),
                               "d2h_bytes": int(d3.nbytes)}
     out["reference_formulas"] = ref
+    # the reference's ASCII coordinate format: parallel host parse, and the
+    # device loader with pinned, overlapped copies
+    import tempfile
+    import torch
+    from entropical_gb300 import read_coords
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "coords.txt")
+        np.savetxt(path, xm.T, fmt="%.8g")
+        size = os.path.getsize(path)
+        t0 = time.perf_counter()
+        host = read_coords(path)
+        t_host = time.perf_counter() - t0
+        dev = torch.empty(host.shape, dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.load_coords_device(path, dev.data_ptr())
+        torch.cuda.synchronize()
+        t_dev = time.perf_counter() - t0
+        same = bool(torch.equal(dev.cpu(), torch.from_numpy(host)))
+    out["coords_file_64x100k"] = {"bytes": size, "read_s": t_host,
+                                  "read_MB_per_s": size / t_host / 1e6, "load_device_s": t_dev,
+                                  "load_device_MB_per_s": size / t_dev / 1e6,
+                                  "device_equals_host": same, "threads": os.cpu_count()}
     return out
 
 

@@ -8,7 +8,8 @@ built on them. There is no CPU implementation of any of these here.
 """
 from ._build import build, lib_path  # noqa: F401
 from ._native import NativeError  # noqa: F401
-from .densities import COMPAT_NORM, Context, as_colmajor, combined_densities, default_context  # noqa: F401
+from .densities import (COMPAT_NORM, Context, as_colmajor, combined_densities,  # noqa: F401
+                        coords_file_shape, default_context, read_coords)
 
 __all__ = [
     "build",
@@ -18,5 +19,7 @@ __all__ = [
     "Context",
     "as_colmajor",
     "combined_densities",
+    "coords_file_shape",
+    "read_coords",
     "default_context",
 ]

@@ -73,6 +73,12 @@ SIGNATURES: dict[str, tuple] = {
     "ent_dens_all": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, c_f32_p,
                                C.c_uint32, c_u32_p, C.c_uint32, C.c_void_p, c_size_p,
                                c_size_p]),
+    "ent_coords_file_shape": (C.c_int, [C.c_char_p, c_size_p, c_size_p]),
+    "ent_read_coords": (C.c_int, [C.c_char_p, c_size_p, C.c_size_t, C.c_char, C.c_void_p,
+                                  C.c_size_t, C.c_size_t]),
+    "ent_load_coords_device": (C.c_int, [C.c_void_p, C.c_char_p, c_size_p, C.c_size_t,
+                                         C.c_void_p, C.c_size_t, C.c_size_t]),
+    "ent_io_last_error": (C.c_char_p, []),
     "ent_te_all_pairs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, c_f32_p,
                                    c_u32_p, C.c_size_t, C.c_uint32, c_f64_p]),
     "ent_te_all_pairs_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t,

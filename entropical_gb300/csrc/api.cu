@@ -615,6 +615,7 @@ const char* ent_status_string(int s) {
     case ENT_ERR_TIMEOUT: return "device-side wait timed out";
     case ENT_ERR_TOO_LARGE: return "input too large";
     case ENT_ERR_STATE: return "invalid state";
+    case ENT_ERR_IO: return "coordinate file unreadable or malformed";
   }
   return "unknown status";
 }

@@ -10,12 +10,14 @@ selected points, computed by the CUDA library; invalid selections raise
 from __future__ import annotations
 
 import ctypes as C
+import os
 from typing import Sequence
 
 import numpy as np
 
 from . import _native
-from ._native import CallStats, HestStats, Instance, c_f32_p, c_f64_p, c_size_p, c_u32_p
+from ._native import (CallStats, HestStats, Instance, NativeError, c_f32_p, c_f64_p, c_size_p,
+                      c_u32_p)
 
 COMPAT_NORM = 1
 BATCH_SUPPORT_COUNTS = 2
@@ -45,6 +47,47 @@ def as_colmajor(coords, n_rows: int | None = None) -> tuple[np.ndarray, int, int
         raise ValueError("coords must be 1-D (flat) or 2-D (n_cols, n_rows)")
     flat = np.ascontiguousarray(a, dtype=np.float32).reshape(-1)
     return flat, int(n_rows), int(n_cols)
+
+
+def _usecols(usecols):
+    if usecols is None or len(usecols) == 0:
+        return None
+    return np.ascontiguousarray(np.asarray(usecols, dtype=np.uintp))
+
+
+def _io_check(st: int) -> None:
+    if st != 0:
+        lib = _native.load()
+        raise NativeError(st, (lib.ent_io_last_error() or b"").decode() or
+                          lib.ent_status_string(st).decode())
+
+
+def coords_file_shape(path) -> tuple[int, int]:
+    """(n_rows, n_cols) of a coordinate file in the reference's ASCII format."""
+    lib = _native.load()
+    r, c = C.c_size_t(), C.c_size_t()
+    _io_check(lib.ent_coords_file_shape(os.fsencode(path), C.byref(r), C.byref(c)))
+    return r.value, c.value
+
+
+def read_coords(path, usecols=None, primary: str = "C") -> np.ndarray:
+    """Tools::IO::read_coords (tools.hxx:153-235), parsed by all host threads.
+    primary 'C' returns the column-major matrix as an (n_cols, n_rows) array
+    (one row per coordinate, the layout the other calls take); 'R' returns
+    (n_rows, n_cols). usecols keep the file's column order."""
+    lib = _native.load()
+    n_rows, n_all = coords_file_shape(path)
+    uc = _usecols(usecols)
+    n_cols = n_all if uc is None else len(set(int(c) for c in uc))
+    if uc is not None and np.any(uc >= n_all):
+        raise NativeError(4, f"given column index is not compatible with available number "
+                             f"of columns ({n_all})")
+    out = np.empty((n_cols, n_rows) if primary == "C" else (n_rows, n_cols), dtype=np.float32)
+    _io_check(lib.ent_read_coords(os.fsencode(path),
+                                  None if uc is None else uc.ctypes.data_as(c_size_p),
+                                  0 if uc is None else len(uc), primary.encode(),
+                                  out.ctypes.data_as(C.c_void_p), n_rows, n_cols))
+    return out
 
 
 def _u32(v: Sequence[int]) -> np.ndarray:
@@ -304,6 +347,18 @@ class Context:
             out.ctypes.data_as(C.c_void_p), C.byref(ni), C.byref(ns))
         self.check(st)
         return out[: ni.value, : ns.value]
+    def load_coords_device(self, path, d_out: int, usecols=None) -> tuple[int, int]:
+        """Parse a coordinate file into the column-major device matrix at
+        address d_out (n_rows x n_cols floats; see coords_file_shape), with
+        pinned, overlapped host-to-device copies. Returns (n_rows, n_cols)."""
+        n_rows, n_all = coords_file_shape(path)
+        uc = _usecols(usecols)
+        n_cols = n_all if uc is None else len(set(int(c) for c in uc))
+        st = self._lib.ent_load_coords_device(
+            self._h, os.fsencode(path), None if uc is None else uc.ctypes.data_as(c_size_p),
+            0 if uc is None else len(uc), C.c_void_p(d_out), n_rows, n_cols)
+        self.check(st)
+        return n_rows, n_cols
 
     # ---------------------------------------------------- neighbour search
     def neighbor_windows(self, col, h: float) -> tuple[np.ndarray, np.ndarray]:

@@ -39,7 +39,8 @@ enum ent_status {
   ENT_ERR_NO_DEVICE = 7,   /* no CUDA device (density_1d.cuh:306-309) */
   ENT_ERR_TIMEOUT = 8,     /* a bounded device-side wait expired */
   ENT_ERR_TOO_LARGE = 9,   /* more rows than 32-bit point indices allow */
-  ENT_ERR_STATE = 10       /* call not valid in the current state */
+  ENT_ERR_STATE = 10,      /* call not valid in the current state */
+  ENT_ERR_IO = 11          /* coordinate file unreadable or malformed */
 };
 
 /* flags for ent_densities* */
@@ -191,6 +192,33 @@ typedef struct {
  */
 int ent_entropy_batch(ent_ctx* ctx, const ent_instance* inst, size_t n_inst,
                       uint32_t flags, double* h_out);
+
+/* ------------------------------------------------------ coordinate files */
+
+/*
+ * The reference's ASCII coordinate format (Tools::IO::read_coords,
+ * tools.hxx:153-235): whitespace-separated values, one row per non-empty
+ * line, n_cols = number of values on the first non-empty line. Read once and
+ * parsed by all host threads (correctly rounded, as `ifs >> float`). A row
+ * with another number of values, or a token that is not a number, is
+ * ENT_ERR_IO (the reference reads across line ends instead). usecols
+ * (nullable, n_usecols = 0: all columns) keep the file's column order, as the
+ * reference does; an index >= n_cols is ENT_ERR_ARG.
+ */
+int ent_coords_file_shape(const char* path, size_t* n_rows, size_t* n_cols);
+/* primary_index 'C': out[c * n_rows + r] (the reference's column-major
+ * layout); 'R': out[r * n_cols_out + c]. n_rows / n_cols_out must match the
+ * file and the selection. */
+int ent_read_coords(const char* path, const size_t* usecols, size_t n_usecols,
+                    char primary_index, float* out, size_t n_rows, size_t n_cols_out);
+/* Same, column-major into device memory d_out of ctx's device: blocks of rows
+ * are parsed into pinned buffers and copied with one 2-D copy per block while
+ * the next block is parsed. */
+int ent_load_coords_device(ent_ctx* ctx, const char* path, const size_t* usecols,
+                           size_t n_usecols, float* d_out, size_t n_rows,
+                           size_t n_cols_out);
+/* Message of the last failing file call of this thread (empty if none). */
+const char* ent_io_last_error(void);
 
 /* ------------------------------------ the reference's estimator formulas */
 

@@ -14,6 +14,7 @@ transfer entropy) on oracle densities.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import subprocess
 from pathlib import Path
 
@@ -330,6 +331,22 @@ def ref_boxedsearch(col: np.ndarray, box: float):
     c = np.empty(len(col), np.uint64)
     nb = ref().ref_boxedsearch(_p(col), C.c_size_t(len(col)), C.c_float(box), _p(b), _p(c))
     return int(nb), c
+
+
+def ref_read_coords(path, primary: str = "C", usecols=None) -> np.ndarray:
+    """The reference's Tools::IO::read_coords (tools.hxx:153-235), compiled in
+    place: 'C' -> (n_cols, n_rows) array of the column-major buffer, 'R' ->
+    (n_rows, n_cols)."""
+    uc = np.ascontiguousarray(np.asarray([] if usecols is None else usecols, dtype=np.uintp))
+    r, k = C.c_size_t(), C.c_size_t()
+    lib = ref()
+    p = C.c_char_p(os.fsencode(str(path)))
+    lib.ref_read_coords(p, C.c_char(primary.encode()), _p(uc), C.c_size_t(len(uc)), None,
+                        C.byref(r), C.byref(k))
+    out = np.empty((k.value, r.value) if primary == "C" else (r.value, k.value), np.float32)
+    lib.ref_read_coords(p, C.c_char(primary.encode()), _p(uc), C.c_size_t(len(uc)), _p(out),
+                        C.byref(r), C.byref(k))
+    return out
 
 
 def ref_thumb(col: np.ndarray) -> float:

@@ -96,4 +96,20 @@ float ref_amise_h(float* coords, std::size_t n_rows, std::size_t i_col) {
   return Hestimate::AmiseMin::Kernel()(coords, n_rows, i_col);
 }
 
+// Tools::IO::read_coords (tools.hxx:153-235): shape of the file (out == null)
+// or its values, column-major ('C') or row-major ('R'), for the used columns.
+int ref_read_coords(const char* path, char primary, const std::size_t* usecols,
+                    std::size_t n_usecols, float* out, std::size_t* n_rows,
+                    std::size_t* n_cols) {
+  std::vector<std::size_t> uc(usecols, usecols + n_usecols);
+  float* c;
+  std::size_t r, k;
+  std::tie(c, r, k) = Tools::IO::read_coords<float>(path, primary, uc);
+  *n_rows = r;
+  *n_cols = k;
+  if (out) std::memcpy(out, c, sizeof(float) * r * k);
+  Tools::IO::free_coords(c);
+  return 0;
+}
+
 }  // extern "C"
