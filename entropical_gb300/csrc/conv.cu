@@ -182,6 +182,9 @@ __global__ void k_conv_plan(const ConvCol* __restrict__ cols, uint32_t n_cols,
       const uint32_t m = e + (f - e) / 2;
       if (C.xs[m] <= vhi) e = m + 1; else f = m;
     }
+    // symmetric: sources before the tile belong to earlier tiles, which
+    // count each such pair twice (k_conv weights)
+    a = max(a, tb);
     td.t_begin = tb;
     td.t_count = tc;
     td.n_runs = 1;
@@ -193,7 +196,11 @@ __global__ void k_conv_plan(const ConvCol* __restrict__ cols, uint32_t n_cols,
 
 // One pass over (target, source) pairs within the window evaluates the
 // convolution kernel at NP bandwidths (NP = 1: plain epa_convolution,
-// NP = 2: both pivots of a search level).
+// NP = 2: both pivots of a search level). The double sum is symmetric in
+// (i, j), so a tile of targets [tb, tb + tc) sees only sources from tb on:
+// sources inside the tile count once (both orders are target-side pairs),
+// sources after it count twice (weight 2, exact), sources before it are
+// counted by their own tile.
 template <int NP, int R>
 __global__ void __launch_bounds__(128)
     k_conv(const TileDesc* __restrict__ tiles, uint32_t n_slots,
@@ -276,6 +283,9 @@ __global__ void __launch_bounds__(128)
         const float* B = bufs + (size_t)b * CC::CAP;
         for (uint32_t pi = 0; pi < npc[b]; ++pi) {
           const uint32_t s0 = ptab[b][pi].s0, n = ptab[b][pi].n;
+          // sorted position of the piece's first element
+          const uint32_t a0 = ptab[b][pi].g0 + (s0 - ptab[b][pi].o);
+          const uint32_t tend = tb + tc;
           if constexpr (NP == 1) {
             float acc[R];
 #pragma unroll
@@ -283,10 +293,11 @@ __global__ void __launch_bounds__(128)
 #pragma unroll 2
             for (uint32_t k = lane; k < n; k += 32) {
               const float s = B[s0 + k];
+              const float wgt = a0 + k >= tend ? 2.f : 1.f;
 #pragma unroll
               for (int r = 0; r < R; ++r) {
                 const float t = fabsf(T[r] - s);
-                acc[r] += fmaxf(fmaf(t, coef[0], 4.5f), 0.f);
+                acc[r] = fmaf(fmaxf(fmaf(t, coef[0], 4.5f), 0.f), wgt, acc[r]);
               }
             }
 #pragma unroll
@@ -300,13 +311,15 @@ __global__ void __launch_bounds__(128)
 #pragma unroll 2
             for (uint32_t k = lane; k < n; k += 32) {
               const float s = B[s0 + k];
+              const float wgt = a0 + k >= tend ? 2.f : 1.f;
+              const f32x2 W = pk2(wgt, wgt);
 #pragma unroll
               for (int r = 0; r < R; ++r) {
                 const float t = fabsf(T[r] - s);
                 const f32x2 w = fma2(pk2(t, t), CO, F45);
                 float w0, w1;
                 upk2(w, w0, w1);
-                acc[r] = add2(acc[r], pk2(fmaxf(w0, 0.f), fmaxf(w1, 0.f)));
+                acc[r] = fma2(pk2(fmaxf(w0, 0.f), fmaxf(w1, 0.f)), W, acc[r]);
               }
             }
 #pragma unroll
