@@ -318,8 +318,8 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
       }
       I.n_strips = I.ncell1 * I.ncell2;
       max_strips = std::max(max_strips, I.n_strips);
-      I.tt = (uint32_t)density_tile_targets(
-          (int)s.d, sym_d[d] ? sym_tile_r(d, var_d[d]) : c.tile_r[s.d - 1]);
+      I.tt = (uint32_t)(sym_d[d] ? sym_tile_targets(d, var_d[d])
+                                 : density_tile_targets((int)s.d, c.tile_r[s.d - 1]));
       I.tile_cap = (s.n + I.tt - 1) / I.tt + std::min(I.n_strips, s.n);
       I.tile_base = slot;
       slot += I.tile_cap;

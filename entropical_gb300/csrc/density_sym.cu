@@ -30,19 +30,20 @@ namespace {
 constexpr unsigned FULL = 0xffffffffu;
 
 // Staged elements per chunk; shared memory per CTA = chunk buffers x 2 plus
-// one float row per warp (4 x CAP floats): 51 KB (d = 1, 2) and 38 KB (d = 3),
-// so that 4 resp. 5 CTAs fit an SM.
-template <int D>
+// one float row per warp (NW x CAP floats). 4 warps: 51 KB (d = 1, 2) and
+// 38 KB (d = 3), 4 resp. 5 CTAs per SM; 8 warps: 44 / 51 / 34 KB, 3 CTAs.
+template <int D, int NW>
 struct SymChunk {
-  static constexpr int CH = D == 1 ? 2048 : (D == 2 ? 1536 : 768);
+  static constexpr int CH = NW == 4 ? (D == 1 ? 2048 : (D == 2 ? 1536 : 768))
+                                    : (D == 1 ? 1024 : (D == 2 ? 1024 : 512));
 };
 
-template <int D, int R, int MINB>
-__global__ void __launch_bounds__(128, MINB)
+template <int D, int R, int MINB, int NW>
+__global__ void __launch_bounds__(NW * 32, MINB)
     k_density_sym(const TileDesc* __restrict__ tiles, uint32_t n_slots,
                   const InstDev* __restrict__ insts, uint32_t* work_counter,
                   uint32_t* err) {
-  typedef Cfg<D, R, SymChunk<D>::CH> C;
+  typedef Cfg<D, R, SymChunk<D, NW>::CH, NW> C;
   typedef typename C::P P;
   static_assert(R <= 32 && (R & (R - 1)) == 0, "R: power of two <= 32");
   extern __shared__ __align__(128) unsigned char dsm[];
@@ -229,7 +230,9 @@ __global__ void __launch_bounds__(128, MINB)
         for (uint32_t k = tid; k < p.n; k += C::NT) {
           if (a + k < tend) continue;
           const uint32_t e = p.s0 + k;
-          const float v = (srow[e] + srow[C::CAP + e]) + (srow[2 * C::CAP + e] + srow[3 * C::CAP + e]);
+          float v = srow[e];
+#pragma unroll
+          for (int w = 1; w < NW; ++w) v += srow[(size_t)w * C::CAP + e];
           if (v != 0.f) atomicAdd(acc64 + a + k, f32_to_f64_int(v));
         }
       }
@@ -248,13 +251,12 @@ __global__ void __launch_bounds__(128, MINB)
   }
 }
 
-template <int D, int R, int MINB>
+template <int D, int R, int MINB, int NW>
 cudaError_t launch_sym_t(cudaStream_t st, const TileDesc* tiles, uint32_t n_slots,
                          const InstDev* insts, uint32_t* work_counter, uint32_t* err,
                          int n_sms, int* launched) {
-  typedef Cfg<D, R, SymChunk<D>::CH> C;
-  auto kern = k_density_sym<D, R, MINB>;
-  static_assert(C::NW == 4, "four warp rows");
+  typedef Cfg<D, R, SymChunk<D, NW>::CH, NW> C;
+  auto kern = k_density_sym<D, R, MINB, NW>;
   const size_t smem = C::SMEM + (size_t)C::NW * C::CAP * sizeof(float);
   cudaError_t e =
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -304,28 +306,32 @@ __global__ void __launch_bounds__(256)
 
 }  // namespace
 
-// Targets per warp of the symmetric bodies: PAIR_SYM 32 (d = 1, 2; 4 CTAs
-// per SM) / 16 (d = 3; 5 CTAs per SM); PAIR_SYM + 1 16 / 8 at 5 CTAs per SM.
+// Shapes of the symmetric bodies: PAIR_SYM 4 warps of 32 targets (d = 1, 2;
+// 4 CTAs per SM) / 16 (d = 3; 5 CTAs per SM); PAIR_SYM + 1 8 warps of 16 /
+// 8 targets, 3 CTAs per SM. Tiles: 128 targets (d = 1, 2), 64 (d = 3).
 int sym_tile_r(int d, int v) {
   if (v == PAIR_SYM) return d == 3 ? 16 : 32;
   return d == 3 ? 8 : 16;
 }
+
+int sym_tile_targets(int d, int v) { return (v == PAIR_SYM ? 4 : 8) * sym_tile_r(d, v); }
 
 cudaError_t launch_density_sym(cudaStream_t st, int d, int v, const TileDesc* tiles,
                                uint32_t n_slots, const InstDev* insts,
                                uint32_t* work_counter, uint32_t* err, int n_sms,
                                int* launched) {
   const int r = sym_tile_r(d, v);
-#define ENT_SYM(D, R, M)                                                               \
-  if (d == D && r == R)                                                                \
-    return launch_sym_t<D, R, M>(st, tiles, n_slots, insts, work_counter, err, n_sms, \
-                                 launched);
-  ENT_SYM(1, 32, 4)
-  ENT_SYM(1, 16, 5)
-  ENT_SYM(2, 32, 4)
-  ENT_SYM(2, 16, 5)
-  ENT_SYM(3, 16, 5)
-  ENT_SYM(3, 8, 5)
+  const int nw = v == PAIR_SYM ? 4 : 8;
+#define ENT_SYM(D, R, M, W)                                                               \
+  if (d == D && r == R && nw == W)                                                        \
+    return launch_sym_t<D, R, M, W>(st, tiles, n_slots, insts, work_counter, err, n_sms, \
+                                    launched);
+  ENT_SYM(1, 32, 4, 4)
+  ENT_SYM(1, 16, 3, 8)
+  ENT_SYM(2, 32, 4, 4)
+  ENT_SYM(2, 16, 3, 8)
+  ENT_SYM(3, 16, 5, 4)
+  ENT_SYM(3, 8, 3, 8)
 #undef ENT_SYM
   return cudaErrorInvalidValue;
 }

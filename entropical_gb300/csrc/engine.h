@@ -130,6 +130,7 @@ __host__ __device__ constexpr bool pair_is_sym(int v) {
   return v == PAIR_SYM || v == PAIR_SYM + 1;
 }
 int sym_tile_r(int d, int v);
+int sym_tile_targets(int d, int v);
 cudaError_t launch_density_sym(cudaStream_t st, int d, int v, const TileDesc* tiles,
                                uint32_t n_slots, const InstDev* insts,
                                uint32_t* work_counter, uint32_t* err, int n_sms,

@@ -16,10 +16,10 @@ template <> struct PtType<1> { typedef float T; };
 template <> struct PtType<2> { typedef float2 T; };
 template <> struct PtType<3> { typedef float4 T; };
 
-// CHX: elements per staged chunk (0 = default for the dimension)
-template <int D, int R, int CHX = 0>
+// CHX: elements per staged chunk (0 = default for the dimension); NWX warps
+template <int D, int R, int CHX = 0, int NWX = 4>
 struct Cfg {
-  static constexpr int NW = 4;
+  static constexpr int NW = NWX;
   static constexpr int NT = NW * 32;
   static constexpr int TT = NW * R;
   typedef typename PtType<D>::T P;
