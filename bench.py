@@ -56,6 +56,8 @@ def parse():
                     help="skip the supplementary measurements of the other configurations")
     ap.add_argument("--pair-variant", default=None,
                     help="pair body per dimension, e.g. '4,4,4' (default: the library's)")
+    ap.add_argument("--cells-per-h3", type=int, default=0,
+                    help="cells per bandwidth of 3-D strips (1 or 2; default: the library's)")
     ap.add_argument("--coords", type=int, default=N_COORDS,
                     help="coordinates of the MI batch (64 = the benchmark workload; "
                          "smaller values give the small case used for ncu captures)")
@@ -367,6 +369,8 @@ def main():
     ctx = Context(local)
     if args.pair_variant:
         ctx.set_tuning(pair_variant=[int(v) for v in args.pair_variant.split(",")])
+    if args.cells_per_h3:
+        ctx.set_tuning(cells_per_h3=args.cells_per_h3)
     var2 = ctx.tuning()["pair_variant_by_dim"][1]
     n_sms = torch.cuda.get_device_properties(local).multi_processor_count
     dx = torch.from_numpy(x).cuda(local)

@@ -2,7 +2,7 @@
 
 The persistent pair kernel has three knobs per density dimension d: targets
 per warp R (tile = 4 R targets), cells per bandwidth S along dimension 1 of
-2-D strips, and the pair body (0: packed sub/fma + min; 1: saturating FMA;
+2-D strips (dimensions 1 and 2 of 3-D strips), and the pair body (0: packed sub/fma + min; 1: saturating FMA;
 2: saturating at 5 CTAs/SM; 3: as 2 with larger chunks; 4: symmetric, each
 unordered pair once, at 5 CTAs/SM; 5: symmetric at 4 CTAs/SM).
 ``tune`` times every supported combination on a sample of the caller's own
@@ -24,8 +24,18 @@ CANDIDATES = {
     1: [(8, 2, 0), (16, 2, 0), (16, 2, 1), (16, 2, 2), (16, 2, 3), (16, 2, 4), (16, 2, 5)],
     2: [(8, 2, 0), (16, 1, 2), (16, 2, 0), (16, 2, 1), (16, 2, 2), (16, 2, 3),
         (16, 1, 4), (16, 2, 4), (16, 2, 5)],
-    3: [(4, 2, 0), (8, 2, 0), (8, 2, 1), (8, 2, 2), (8, 2, 3), (8, 2, 4), (8, 2, 5)],
+    3: [(4, 1, 0), (8, 1, 0), (8, 1, 1), (8, 1, 2), (8, 2, 2), (8, 1, 3), (8, 1, 4), (8, 2, 4),
+        (8, 2, 5)],
 }
+
+
+def _set(ctx: Context, tpw, d: int, s: int, pv) -> None:
+    # s: cells per bandwidth of the strips (dimension 1 for d = 2, dimensions
+    # 1 and 2 for d = 3; unused for d = 1)
+    if d == 3:
+        ctx.set_tuning(tpw, 0, pv, cells_per_h3=s)
+    else:
+        ctx.set_tuning(tpw, s, pv)
 
 
 def cache_path() -> Path:
@@ -79,7 +89,7 @@ def tune(ctx: Context, run, d: int, n: int, repeats: int = 2, save: bool = True)
         tpw[d - 1] = r
         pv = [None, None, None]
         pv[d - 1] = v
-        ctx.set_tuning(tpw, s, pv)
+        _set(ctx, tpw, d, s, pv)
         run()  # warm-up (all variants are prebuilt)
         best = math.inf
         for _ in range(repeats):
@@ -91,7 +101,7 @@ def tune(ctx: Context, run, d: int, n: int, repeats: int = 2, save: bool = True)
     tpw[d - 1] = r
     pv = [None, None, None]
     pv[d - 1] = v
-    ctx.set_tuning(tpw, s, pv)
+    _set(ctx, tpw, d, s, pv)
     choice = {"targets_per_warp": r, "cells_per_h": s, "pair_variant": v, "ms": best,
               "all": [{"r": rr, "s": ss, "v": vv, "ms": mm} for mm, rr, ss, vv in results]}
     if save:
@@ -110,5 +120,5 @@ def apply(ctx: Context, d: int, n: int) -> bool:
     tpw[d - 1] = c["targets_per_warp"]
     pv = [None, None, None]
     pv[d - 1] = c["pair_variant"]
-    ctx.set_tuning(tpw, c["cells_per_h"], pv)
+    _set(ctx, tpw, d, c["cells_per_h"], pv)
     return True

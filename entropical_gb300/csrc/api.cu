@@ -295,7 +295,8 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
         prod_hg2 *= (double)s.h[j] * (double)I.g2[j];
       }
       I.perm0 = vvals + voff[s.view[0]];
-      I.S = s.d == 2 ? std::max(1u, std::min(4u, s.S)) : 1u;
+      I.S = s.d == 2 ? std::max(1u, std::min(4u, s.S))
+                     : (s.d == 3 ? std::max(1u, std::min(2u, c.strip_subdiv3)) : 1u);
       I.ncell1 = I.ncell2 = 1;
       if (s.d >= 2) {
         const ViewStats& a = vs[s.view[1]];
@@ -310,7 +311,7 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
       }
       if (s.d == 3) {
         const ViewStats& b = vs[s.view[2]];
-        const double w = (double)s.h[2] * (1.0 + 1e-4);
+        const double w = (double)s.h[2] / I.S * (1.0 + 1e-4);
         I.lo2 = b.mn;
         I.inv_w2 = 1.0 / w;
         I.ncell2 = (uint32_t)std::min<double>(
@@ -627,6 +628,7 @@ int ent_set_tuning(ent_ctx* ctx, const ent_tuning* t) {
     if (t->targets_per_warp[d - 1] && !density_r_supported(d, (int)t->targets_per_warp[d - 1]))
       return c->fail(ENT_ERR_ARG, "unsupported targets_per_warp");
   if (t->cells_per_h > 4) return c->fail(ENT_ERR_ARG, "cells_per_h must be 1..4");
+  if (t->cells_per_h3 > 2) return c->fail(ENT_ERR_ARG, "cells_per_h3 must be 1..2");
   if (t->pair_variant > PAIR_SYM + 2) return c->fail(ENT_ERR_ARG, "pair_variant must be 0..6");
   for (int d = 0; d < 3; ++d)
     if (t->pair_variant_by_dim[d] > PAIR_SYM + 2)
@@ -638,6 +640,7 @@ int ent_set_tuning(ent_ctx* ctx, const ent_tuning* t) {
   for (int d = 1; d <= 3; ++d)
     if (t->targets_per_warp[d - 1]) c->tile_r[d - 1] = (int)t->targets_per_warp[d - 1];
   if (t->cells_per_h) c->strip_subdiv = t->cells_per_h;
+  if (t->cells_per_h3) c->strip_subdiv3 = t->cells_per_h3;
   return ENT_OK;
 }
 
@@ -646,6 +649,7 @@ int ent_get_tuning(const ent_ctx* ctx, ent_tuning* t) {
   const Ctx* c = reinterpret_cast<const Ctx*>(ctx);
   for (int d = 0; d < 3; ++d) t->targets_per_warp[d] = (uint32_t)c->tile_r[d];
   t->cells_per_h = c->strip_subdiv;
+  t->cells_per_h3 = c->strip_subdiv3;
   t->pair_variant = (uint32_t)c->pair_variant[1] + 1;
   for (int d = 0; d < 3; ++d) t->pair_variant_by_dim[d] = (uint32_t)c->pair_variant[d] + 1;
   return ENT_OK;

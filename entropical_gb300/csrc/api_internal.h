@@ -39,6 +39,7 @@ struct Ctx {
   ent_call_stats stats{};
   bool pending_pairs = false;
   uint32_t strip_subdiv = 2;  // cells per bandwidth along dimension 1 (d = 2)
+  uint32_t strip_subdiv3 = 1;  // cells per bandwidth along dimensions 1, 2 (d = 3)
   int tile_r[3] = {16, 16, 8};  // targets per warp of the pair kernel, by d
   // pair body per dimension: 0 min-based, 1 saturating FMA, 2 saturating at
   // 5 CTAs/SM, 3 as 2 with larger chunks (fastest measured: 2, 2, 1)

@@ -27,7 +27,9 @@ cudaError_t seg_radix_sort(cudaStream_t st, const SegTableDev& t,
                            uint32_t*& vtmp, int begin_bit, int end_bit);
 
 // -------------------------------------------------------- density engine
-constexpr int MAX_RUNS = 9;  // 3 cells per remaining dimension, d <= 3
+// candidate runs per tile: 2S+1 strips for d = 2 (S <= 4 cells per
+// bandwidth), (2S+1)^2 for d = 3 (S <= 2)
+constexpr int MAX_RUNS = 25;
 
 // One column view: a contiguous float32 range on the device (a selected,
 // possibly lagged coordinate column).

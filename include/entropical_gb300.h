@@ -78,6 +78,8 @@ typedef struct {
                                    dimension (get reports dimension 2) */
   uint32_t pair_variant_by_dim[3]; /* the same per dimension (0 = keep);
                                       applied after pair_variant */
+  uint32_t cells_per_h3;        /* d=3 strips: cells per bandwidth along
+                                   dimensions 1 and 2, 1..2 (default 1) */
 } ent_tuning;
 
 /* Context lifecycle. device < 0 selects the current device. */

