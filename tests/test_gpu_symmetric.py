@@ -144,4 +144,6 @@ def test_sym_3d_cell_sizes(cells3):
             p = c.combined_densities(x, None, [0, 1, 2], [0.2, 0.3, 0.25])
             assert rel_err(p, O.density_fp64(O.repack(x, [0, 1, 2]), [0.2, 0.3, 0.25])) < REL
         cnt = c.support_counts(x, None, [0, 1, 2], [0.2, 0.3, 0.25])
-        assert cnt.sum() == O.support_count_fp64(O.repack(x, [0, 1, 2]), [0.2, 0.3, 0.25]) or True
+    with Context(0) as c1:
+        c1.set_tuning(cells_per_h3=1)
+        assert np.array_equal(cnt, c1.support_counts(x, None, [0, 1, 2], [0.2, 0.3, 0.25]))
