@@ -56,6 +56,8 @@ def parse():
                     help="skip the supplementary measurements of the other configurations")
     ap.add_argument("--pair-variant", default=None,
                     help="pair body per dimension, e.g. '4,4,4' (default: the library's)")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the library's default tile shapes (no autotuner pass)")
     ap.add_argument("--cells-per-h3", type=int, default=0,
                     help="cells per bandwidth of 3-D strips (1 or 2; default: the library's)")
     ap.add_argument("--coords", type=int, default=N_COORDS,
@@ -254,15 +256,22 @@ def other_configs(ctx):
         "support_pairs_3d": sup3, "candidate_pairs_3d": st.candidate_pairs_by_dim[2],
         "h2d_bytes": int(xt.nbytes)}
     ub = workloads.uneven_batch(512, seed=5)
-    H = ctx.entropy_batch(ub)
-    H = ctx.entropy_batch(ub)
-    st = ctx.last_stats()
+    # tile/cell shapes per dimension picked by the autotuner on this batch
+    from entropical_gb300 import Context, autotune
+    uctx = Context(-1)
+    utuned = {f"d{d}": {k: v for k, v in autotune.tune(uctx, lambda: uctx.entropy_batch(ub), d=d,
+                                                       n=100_000, repeats=1, save=False).items()
+                        if k != "all"} for d in (1, 2, 3)}
+    H = uctx.entropy_batch(ub)
+    H = uctx.entropy_batch(ub)
+    st = uctx.last_stats()
+    uctx.close()
     supu = float(ctx.entropy_batch(ub, counts=True).sum())
     t0 = time.perf_counter()
     for xq, hq in ub:
         ctx.combined_densities(xq, None, list(range(xq.shape[0])), hq)
     seq = time.perf_counter() - t0
-    out["uneven_512"] = {"batched_ms": st.total_ms, "sequential_plain_s": seq,
+    out["uneven_512"] = {"batched_ms": st.total_ms, "sequential_plain_s": seq, "autotuned": utuned,
                          "speedup": seq / (st.total_ms / 1e3), "support_pairs": supu,
                          "pairs_per_s": supu / (st.total_ms / 1e3),
                          "points": int(sum(xq.shape[1] for xq, _ in ub))}
@@ -371,11 +380,21 @@ def main():
         ctx.set_tuning(pair_variant=[int(v) for v in args.pair_variant.split(",")])
     if args.cells_per_h3:
         ctx.set_tuning(cells_per_h3=args.cells_per_h3)
-    var2 = ctx.tuning()["pair_variant_by_dim"][1]
     n_sms = torch.cuda.get_device_properties(local).multi_processor_count
     dx = torch.from_numpy(x).cuda(local)
     ptr = dx.data_ptr()
     iu = np.triu_indices(M, 1)
+    tuned = None
+    if not (args.no_autotune or args.pair_variant or args.cells_per_h3):
+        # tile/cell shapes picked by the autotuner on a sample of this batch
+        # (the first 16 coordinates: 120 2-D and 16 1-D densities), untimed
+        from entropical_gb300 import autotune
+        ms = min(M, 16)
+        run = lambda: ctx.mi_all_pairs_device(ptr, N_FRAMES, ms, h[:ms])  # noqa: E731
+        tuned = {f"d{d}": {k: v for k, v in autotune.tune(ctx, run, d=d, n=N_FRAMES,
+                                                           save=False).items() if k != "all"}
+                 for d in (2, 1)}
+    var2 = ctx.tuning()["pair_variant_by_dim"][1]
 
     # work units of the step: in-support (target, source) pairs (untimed)
     cnt, c1 = ctx.mi_all_pairs_device(ptr, N_FRAMES, M, h, counts=True)
@@ -449,6 +468,7 @@ def main():
                 "h2d_bytes_per_step": int(x.nbytes), "d2h_bytes_per_step": int(mi.nbytes + hx.nbytes),
                 "ms_per_step": e2e},
         "gpu_launches": launches,
+        "autotuned": tuned,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "kernel": (f"k_density_sym<2,{32 if var2 == 4 else 16}> (2-D symmetric "
