@@ -327,6 +327,33 @@ class Context:
         self.check(st)
         return out if vec else out.reshape(n_cols, n_cols)
 
+    def reference_estimator_device(self, d_coords: int, n_rows: int, n_cols: int,
+                                   h: Sequence[float], estimator: int, tau: int = 0
+                                   ) -> np.ndarray:
+        """reference_estimator on a column-major device matrix (raw address)."""
+        hv = _f32(h)
+        vec = estimator in (REF_AUTOENT, REF_NEGS)
+        out = np.zeros(n_cols if vec else n_cols * n_cols, dtype=np.float64)
+        st = self._lib.ent_reference_estimator(
+            self._h, C.c_void_p(d_coords), n_rows, n_cols, hv.ctypes.data_as(c_f32_p),
+            int(estimator), int(tau), BATCH_DEVICE_INPUT, out.ctypes.data_as(c_f64_p))
+        self.check(st)
+        return out if vec else out.reshape(n_cols, n_cols)
+
+    def dens_all_device(self, d_coords: int, n_rows: int, n_cols: int, h: Sequence[float],
+                        dims: int, d_out: int, taus=None) -> tuple[int, int]:
+        """dens_all with device coordinates and device output (raw addresses;
+        d_out holds n_densities x n_sel doubles). Returns (n_densities, n_sel)."""
+        hv = _f32(h)
+        tv = None if taus is None else _u32(taus)
+        ni, ns = C.c_size_t(), C.c_size_t()
+        st = self._lib.ent_dens_all(
+            self._h, C.c_void_p(d_coords), n_rows, n_cols, hv.ctypes.data_as(c_f32_p), int(dims),
+            None if tv is None else tv.ctypes.data_as(c_u32_p),
+            BATCH_DEVICE_INPUT | BATCH_DEVICE_OUTPUT, C.c_void_p(d_out), C.byref(ni), C.byref(ns))
+        self.check(st)
+        return ni.value, ns.value
+
     def dens_all(self, coords, h: Sequence[float], dims: int, taus=None) -> np.ndarray:
         """Sum-normalised densities of every column (dims=1), pair (2) or
         triple (3) in the reference's order (dens.cpp:19-106), one device

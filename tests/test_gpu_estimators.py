@@ -101,3 +101,18 @@ def test_estimator_argument_errors(ctx):
         ctx.reference_estimator(x, [0.1, -1.0], 1)
     with pytest.raises(NativeError):
         ctx.dens_all(x, [0.1, 0.1], 4)
+
+
+def test_device_input_and_output_forms(ctx):
+    torch = pytest.importorskip("torch")
+    x = workloads.mi_coords(3000, 4, seed=9)
+    h = workloads.scott_bandwidth(x, 2)
+    dx = torch.from_numpy(np.ascontiguousarray(x)).cuda()
+    for kind, tau in ((1, 0), (2, 2), (3, 3), (4, 0), (5, 0)):
+        r_dev = ctx.reference_estimator_device(dx.data_ptr(), 3000, 4, h, kind, tau)
+        assert np.allclose(r_dev, ctx.reference_estimator(x, h, kind, tau), rtol=1e-12, atol=1e-15)
+    out = torch.zeros((4, 2999), dtype=torch.float64, device="cuda")
+    ni, ns = ctx.dens_all_device(dx.data_ptr(), 3000, 4, h, 3, out.data_ptr(), [0, 1, 0])
+    torch.cuda.synchronize()
+    assert (ni, ns) == (4, 2999)
+    assert np.allclose(out.cpu().numpy(), ctx.dens_all(x, h, 3, [0, 1, 0]), rtol=1e-12, atol=0)
