@@ -117,6 +117,28 @@ int Ctx::end_call() {
   return ENT_OK;
 }
 
+// Table of log_fp64 (common.cuh), computed with the host's libm.
+cudaError_t init_log_table(double2** out) {
+  std::vector<double2> t(LOG64_TABLE_ENTRIES);
+  for (int k = 0; k < 256; ++k) {
+    const long double c = 1.0L + ((long double)k + 0.5L) / 256.0L;
+    t[k].x = (double)(1.0L / c);
+    t[k].y = (double)std::log(c);
+  }
+  const long double ln2 = std::log(2.0L);
+  const double hi = (double)ln2;
+  unsigned long long hb;
+  std::memcpy(&hb, &hi, sizeof(hb));
+  hb &= 0xffffffff00000000ull;
+  double hi32;
+  std::memcpy(&hi32, &hb, sizeof(hi32));
+  t[256].x = hi32;
+  t[256].y = (double)(ln2 - (long double)hi32);
+  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(out), sizeof(double2) * t.size());
+  if (e != cudaSuccess) return e;
+  return cudaMemcpy(*out, t.data(), sizeof(double2) * t.size(), cudaMemcpyHostToDevice);
+}
+
 // ----------------------------------------------------------------- engine
 namespace {
 
@@ -467,7 +489,7 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
       c.ran_d[d - 1] = true;
       launches += 1;
       if (sym_d[d]) {
-        r = launch_sym_finish(st, tiles + group_base[d], group_slots[d], di_sorted,
+        r = launch_sym_finish(st, tiles + group_base[d], group_slots[d], di_sorted, c.d_logtab,
                               tile_ls + group_base[d], mode);
         if (r != cudaSuccess) return r;
         launches += 1;
@@ -580,6 +602,11 @@ int ent_create(ent_ctx** out, int device) {
     return ENT_ERR_CUDA;
   }
   if (const char* g = std::getenv("ENT_NO_GRAPHS")) c->use_graphs = (g[0] == '0');
+  if (init_log_table(&c->d_logtab) != cudaSuccess) {
+    cudaGetLastError();
+    ent_destroy(reinterpret_cast<ent_ctx*>(c));
+    return ENT_ERR_CUDA;
+  }
   *out = reinterpret_cast<ent_ctx*>(c);
   return ENT_OK;
 }
@@ -591,6 +618,7 @@ void ent_destroy(ent_ctx* ctx) {
   cudaStreamSynchronize(c->stream);
   c->arena.release();
   cudaFree(c->d_err);
+  if (c->d_logtab) cudaFree(c->d_logtab);
   cudaEventDestroy(c->ev_call0);
   cudaEventDestroy(c->ev_call1);
   cudaEventDestroy(c->ev_k0);
@@ -619,6 +647,22 @@ const char* ent_status_string(int s) {
     case ENT_ERR_IO: return "coordinate file unreadable or malformed";
   }
   return "unknown status";
+}
+
+int ent_log64_selftest(ent_ctx* ctx, const double* x, size_t n, double* out) {
+  if (!ctx || (n && (!x || !out))) return ENT_ERR_ARG;
+  Ctx* c = reinterpret_cast<Ctx*>(ctx);
+  int s = c->begin_call();
+  if (s) return s;
+  if (n == 0) return c->end_call();
+  double* d = static_cast<double*>(c->arena.alloc(2 * sizeof(double) * n));
+  if (!d) return c->fail(ENT_ERR_CUDA, "out of device memory");
+  cudaError_t e = cudaMemcpyAsync(d, x, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = launch_log64_test(c->stream, d, n, c->d_logtab, d + n);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(out, d + n, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream);
+  if (e != cudaSuccess) return c->cuda_fail(e, "log self-test");
+  return c->end_call();
 }
 
 int ent_set_tuning(ent_ctx* ctx, const ent_tuning* t) {

@@ -29,6 +29,7 @@ struct Ctx {
   int n_sms = 1;
   cudaStream_t stream = nullptr;
   uint32_t* d_err = nullptr;
+  double2* d_logtab = nullptr;  // LOG64_TABLE_ENTRIES entries of log_fp64
   cudaEvent_t ev_call0 = nullptr, ev_call1 = nullptr;
   cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr;
   cudaEvent_t ev_d[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};

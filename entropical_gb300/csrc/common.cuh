@@ -144,6 +144,37 @@ __device__ __forceinline__ double f32_to_f64_int(float v) {
   return __longlong_as_double((long long)r);
 }
 
+// Natural log in FP64 for the per-point epilogues, with few FP64 operations
+// (the FP64 pipe of this GPU runs at a small fraction of the FP32 rate).
+// Table reduction (Tang's method): x = m 2^e with m in [1, 2); the top 8 bits
+// of m pick c = 1 + (k + 1/2)/256 with FP64 entries {1/c, log c} (computed on
+// the host, LOG64_TABLE_ENTRIES = 256 + 1: the last one holds log 2 split in a
+// high part with 32 zero low bits, exact in e * hi, and the remainder); then
+// r = m/c - 1 in [-2^-9, 2^-9] and log1p(r) = r - r^2/2 + ... + r^7/7 (the
+// first omitted term is below 2^-66). log x = (e*ln2_hi + log c) +
+// (e*ln2_lo + log1p(r)). Non-normal or non-positive x fall back to log().
+constexpr int LOG64_TABLE_ENTRIES = 257;
+__device__ __forceinline__ double log_fp64(double x, const double2* __restrict__ tab) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned ex = (unsigned)(b >> 52);  // sign and biased exponent
+  if (ex == 0u || ex >= 0x7ffu) return log(x);
+  const int e = (int)ex - 1023;
+  const unsigned k = (unsigned)(b >> 44) & 0xffu;
+  const double m = __longlong_as_double((long long)((b & 0x000fffffffffffffull) |
+                                                    0x3ff0000000000000ull));
+  const double2 t = __ldg(tab + k);  // {1/c, log c}
+  const double2 l2 = __ldg(tab + 256);
+  const double r = fma(m, t.x, -1.0);
+  double p = fma(r, 1.0 / 7.0, -1.0 / 6.0);
+  p = fma(r, p, 1.0 / 5.0);
+  p = fma(r, p, -1.0 / 4.0);
+  p = fma(r, p, 1.0 / 3.0);
+  p = fma(r, p, -0.5);
+  p = fma(r * r, p, r);
+  const double de = (double)e;
+  return fma(de, l2.x, t.y) + fma(de, l2.y, p);
+}
+
 __device__ __forceinline__ uint32_t float_key(float f) {
   uint32_t u = __float_as_uint(f);
   return (u & 0x80000000u) ? ~u : (u | 0x80000000u);

@@ -22,6 +22,8 @@
 //
 // Every mbarrier wait is bounded; on expiry the kernel reports EF_TIMEOUT,
 // waits (bounded) for its own copies in flight and returns.
+#include <algorithm>
+
 #include "staging.cuh"
 
 namespace ent {
@@ -280,8 +282,8 @@ cudaError_t launch_sym_t(cudaStream_t st, const TileDesc* tiles, uint32_t n_slot
 // (log or value) into the slot's tile_logsum.
 __global__ void __launch_bounds__(256)
     k_sym_finish(const TileDesc* __restrict__ tiles, uint32_t n_slots,
-                 const InstDev* __restrict__ insts, double* tile_logsum,
-                 uint32_t mode) {
+                 const InstDev* __restrict__ insts, const double2* __restrict__ logtab,
+                 double* tile_logsum, uint32_t mode) {
   const uint32_t g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (g >= n_slots) return;  // warp-uniform
@@ -294,7 +296,7 @@ __global__ void __launch_bounds__(256)
       const uint32_t k = T.t_begin + li;
       const double dens = I.scale * I.acc[k];
       if (mode & DM_WRITE_F64) I.out[I.perm[k]] = dens;
-      if (mode & DM_LOGSUM) ls += log(dens);
+      if (mode & DM_LOGSUM) ls += log_fp64(dens, logtab);
       else if (mode & DM_SUMV) ls += dens;
     }
   }
@@ -302,6 +304,13 @@ __global__ void __launch_bounds__(256)
     for (int o = 16; o; o >>= 1) ls += __shfl_xor_sync(FULL, ls, o);
     if (lane == 0) tile_logsum[g] = ls;
   }
+}
+
+__global__ void k_log64_test(const double* __restrict__ x, size_t n,
+                             const double2* __restrict__ logtab, double* __restrict__ out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    out[i] = log_fp64(x[i], logtab);
 }
 
 }  // namespace
@@ -338,10 +347,19 @@ cudaError_t launch_density_sym(cudaStream_t st, int d, int v, const TileDesc* ti
 
 cudaError_t launch_sym_finish(cudaStream_t st, const TileDesc* tiles,
                               uint32_t n_slots, const InstDev* insts,
-                              double* tile_logsum, uint32_t mode) {
+                              const double2* logtab, double* tile_logsum, uint32_t mode) {
   if (n_slots == 0) return cudaSuccess;
   const uint64_t blocks = ((uint64_t)n_slots * 32 + 255) / 256;
-  k_sym_finish<<<(unsigned)blocks, 256, 0, st>>>(tiles, n_slots, insts, tile_logsum, mode);
+  k_sym_finish<<<(unsigned)blocks, 256, 0, st>>>(tiles, n_slots, insts, logtab, tile_logsum,
+                                                  mode);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_log64_test(cudaStream_t st, const double* x, size_t n,
+                              const double2* logtab, double* out) {
+  if (n == 0) return cudaSuccess;
+  const unsigned blocks = (unsigned)std::min<size_t>((n + 255) / 256, 4096);
+  k_log64_test<<<blocks, 256, 0, st>>>(x, n, logtab, out);
   return cudaGetLastError();
 }
 

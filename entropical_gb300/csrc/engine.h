@@ -139,7 +139,10 @@ cudaError_t launch_density_sym(cudaStream_t st, int d, int v, const TileDesc* ti
                                int* launched_ctas);
 cudaError_t launch_sym_finish(cudaStream_t st, const TileDesc* tiles,
                               uint32_t n_slots, const InstDev* insts,
-                              double* tile_logsum, uint32_t mode);
+                              const double2* logtab, double* tile_logsum, uint32_t mode);
+// out[i] = log_fp64(x[i]) (device arrays; self-test of the epilogue log)
+cudaError_t launch_log64_test(cudaStream_t st, const double* x, size_t n,
+                              const double2* logtab, double* out);
 cudaError_t launch_inst_logsum(cudaStream_t st, const InstDev* insts,
                                uint32_t n_inst, const double* tile_logsum,
                                double* inst_logsum);

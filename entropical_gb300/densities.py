@@ -327,6 +327,14 @@ class Context:
         self.check(st)
         return out if vec else out.reshape(n_cols, n_cols)
 
+    def log64_selftest(self, x) -> np.ndarray:
+        """The FP64 log of the per-point epilogues evaluated on the device."""
+        xv = np.ascontiguousarray(np.asarray(x, dtype=np.float64).ravel())
+        out = np.empty_like(xv)
+        self.check(self._lib.ent_log64_selftest(self._h, xv.ctypes.data_as(c_f64_p), xv.size,
+                                                 out.ctypes.data_as(c_f64_p)))
+        return out
+
     def reference_estimator_device(self, d_coords: int, n_rows: int, n_cols: int,
                                    h: Sequence[float], estimator: int, tau: int = 0
                                    ) -> np.ndarray:

@@ -90,6 +90,10 @@ const char* ent_status_string(int status);
 const char* ent_last_error(const ent_ctx* ctx);
 int ent_last_stats(const ent_ctx* ctx, ent_call_stats* stats);
 int ent_set_tuning(ent_ctx* ctx, const ent_tuning* tuning);
+/* Diagnostic: out[i] = the FP64 natural log the per-point epilogues use
+ * (a table-reduction log with few FP64 operations), on the device, for n
+ * host values. No counterpart in the reference. */
+int ent_log64_selftest(ent_ctx* ctx, const double* x, size_t n, double* out);
 int ent_get_tuning(const ent_ctx* ctx, ent_tuning* tuning);
 
 /*

@@ -194,3 +194,20 @@ def test_pair_body_variants(d, variant):
         for hv in (1e-6, 50.0):
             p = c.combined_densities(x, None, cols, [hv] * d)
             assert rel_err(p, O.density_fp64(O.repack(x, cols), [hv] * d)) < REL
+
+
+def test_epilogue_log(ctx):
+    """The table-reduction FP64 log of the per-point epilogues is within
+    5e-16 * max(1, |log x|) of the FP64 log (absolute accuracy is what the
+    entropy sums need); non-normal inputs take the library log."""
+    rng = np.random.default_rng(12)
+    x = np.concatenate([10 ** rng.uniform(-300, 300, 100_000), 10 ** rng.uniform(-9, 4, 100_000),
+                        1 + rng.uniform(-1e-3, 1e-3, 5000), 0.5 + rng.uniform(-1e-3, 1e-3, 5000),
+                        2.0 ** np.arange(-1000, 1000, 7), [1.0, 2.0, 0.5, np.nextafter(1, 2)]])
+    y = ctx.log64_selftest(x)
+    ref = np.log(x)
+    assert np.all(np.abs(y - ref) <= 5e-16 * np.maximum(1.0, np.abs(ref)))
+    special = np.array([5e-324, 1e-310, np.inf, 0.0])
+    with np.errstate(divide="ignore"):
+        assert np.allclose(ctx.log64_selftest(special)[:3], np.log(special[:3]), rtol=1e-15)
+    assert ctx.log64_selftest(special)[3] == -np.inf
