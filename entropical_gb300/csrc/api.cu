@@ -649,6 +649,16 @@ const char* ent_status_string(int s) {
   return "unknown status";
 }
 
+int ent_wait_selftest(ent_ctx* ctx) {
+  if (!ctx) return ENT_ERR_ARG;
+  Ctx* c = reinterpret_cast<Ctx*>(ctx);
+  int s = c->begin_call();
+  if (s) return s;
+  cudaError_t e = launch_wait_test(c->stream, c->d_err);
+  if (e != cudaSuccess) return c->cuda_fail(e, "wait self-test");
+  return c->end_call();
+}
+
 int ent_log64_selftest(ent_ctx* ctx, const double* x, size_t n, double* out) {
   if (!ctx || (n && (!x || !out))) return ENT_ERR_ARG;
   Ctx* c = reinterpret_cast<Ctx*>(ctx);

@@ -306,6 +306,19 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// One bounded wait on an mbarrier whose expected bytes never arrive: the
+// wait gives up after ENT_WAIT_NS and the kernel reports EF_TIMEOUT (no copy
+// is in flight, so the CTA may exit).
+__global__ void k_wait_test(uint32_t* err) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+    mbar_arrive_expect_tx(&bar, 16);
+    if (!mbar_wait(&bar, 0)) atomicOr(err, EF_TIMEOUT);
+  }
+}
+
 __global__ void k_log64_test(const double* __restrict__ x, size_t n,
                              const double2* __restrict__ logtab, double* __restrict__ out) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
@@ -352,6 +365,11 @@ cudaError_t launch_sym_finish(cudaStream_t st, const TileDesc* tiles,
   const uint64_t blocks = ((uint64_t)n_slots * 32 + 255) / 256;
   k_sym_finish<<<(unsigned)blocks, 256, 0, st>>>(tiles, n_slots, insts, logtab, tile_logsum,
                                                   mode);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_wait_test(cudaStream_t st, uint32_t* err) {
+  k_wait_test<<<1, 32, 0, st>>>(err);
   return cudaGetLastError();
 }
 

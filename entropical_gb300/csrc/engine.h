@@ -140,6 +140,8 @@ cudaError_t launch_density_sym(cudaStream_t st, int d, int v, const TileDesc* ti
 cudaError_t launch_sym_finish(cudaStream_t st, const TileDesc* tiles,
                               uint32_t n_slots, const InstDev* insts,
                               const double2* logtab, double* tile_logsum, uint32_t mode);
+// a bounded mbarrier wait that runs out: sets EF_TIMEOUT in *err
+cudaError_t launch_wait_test(cudaStream_t st, uint32_t* err);
 // out[i] = log_fp64(x[i]) (device arrays; self-test of the epilogue log)
 cudaError_t launch_log64_test(cudaStream_t st, const double* x, size_t n,
                               const double2* logtab, double* out);

@@ -94,6 +94,10 @@ int ent_set_tuning(ent_ctx* ctx, const ent_tuning* tuning);
  * (a table-reduction log with few FP64 operations), on the device, for n
  * host values. No counterpart in the reference. */
 int ent_log64_selftest(ent_ctx* ctx, const double* x, size_t n, double* out);
+/* Diagnostic of the failure path: one device-side wait that nothing
+ * completes runs into its bound (2 s) and the call returns ENT_ERR_TIMEOUT;
+ * the context stays usable. No counterpart in the reference. */
+int ent_wait_selftest(ent_ctx* ctx);
 int ent_get_tuning(const ent_ctx* ctx, ent_tuning* tuning);
 
 /*

@@ -211,3 +211,19 @@ def test_epilogue_log(ctx):
     with np.errstate(divide="ignore"):
         assert np.allclose(ctx.log64_selftest(special)[:3], np.log(special[:3]), rtol=1e-15)
     assert ctx.log64_selftest(special)[3] == -np.inf
+
+
+def test_bounded_wait_reports_timeout():
+    """A device-side wait that nothing completes gives up after its bound; the
+    call returns ENT_ERR_TIMEOUT and the context keeps working."""
+    import time
+    from entropical_gb300 import Context
+    with Context(0) as c:
+        t0 = time.perf_counter()
+        st = c.lib.ent_wait_selftest(c.handle)
+        dt = time.perf_counter() - t0
+        assert st == 8, st  # ENT_ERR_TIMEOUT
+        assert 1.5 < dt < 30
+        x = np.random.default_rng(3).standard_normal((2, 2000)).astype(np.float32)
+        p = c.combined_densities(x, None, [0, 1], [0.3, 0.3])
+        assert rel_err(p, O.density_fp64(x, [0.3, 0.3])) < REL
