@@ -229,6 +229,64 @@ def compare_plain(ctx, x, ptr, log_fp64_pairs=2):
     return out
 
 
+def compare_plain_te(ctx, n_coords=8, taus=(1, 5, 10)):
+    """Transfer entropy of all ordered pairs over the first n_coords of the
+    coupled-Langevin data (200k frames, 3 lags), bandwidths by the AMISE
+    search, two ways: plain -- per column 16 epa_convolution calls driven by
+    the AmiseMin bracket logic, then one density call per density the TE
+    estimates need (1-D, 2-D lagged, 2-D joint, 3-D; transs.cpp:39-115
+    structure); batched+learned -- ent_hestimate_learned for all columns and
+    one ent_te_all_pairs batch for all pairs and lags."""
+    from entropical_gb300 import learned, workloads
+    from entropical_gb300.densities import HEST_THUMB
+    from entropical_gb300.estimators import hestimate_amise_plain
+    xt, _ = workloads.langevin(32, 200_000, seed=11)
+    x = np.ascontiguousarray(xt[:n_coords])
+    M, N = x.shape
+    sync = __import__("torch").cuda.synchronize
+    sync()
+    t0 = time.perf_counter()
+    h0, _ = ctx.hestimate(x, HEST_THUMB)
+    hp = np.array([hestimate_amise_plain(ctx, x[j], float(h0[j]))[0] for j in range(M)],
+                  np.float32)
+    calls, te_plain = 0, np.zeros((len(taus), M, M))
+    for q, tau in enumerate(taus):
+        n = N - tau
+        xn = np.ascontiguousarray(x[:, :n])  # the n samples t of y_i and x_j
+        H1 = [-np.mean(np.log(ctx.combined_densities(xn, None, [i], [hp[i]])))
+              for i in range(M)]
+        Hl = [-np.mean(np.log(ctx.combined_densities(x, None, [i, i], [hp[i], hp[i]], [tau, 0])))
+              for i in range(M)]
+        calls += 2 * M
+        for i in range(M):
+            for j in range(M):
+                if i == j:
+                    continue
+                H2 = -np.mean(np.log(ctx.combined_densities(xn, None, [i, j],
+                                                            [hp[i], hp[j]])))
+                H3 = -np.mean(np.log(ctx.combined_densities(
+                    x, None, [i, i, j], [hp[i], hp[i], hp[j]], [tau, 0, 0])))
+                calls += 2
+                te_plain[q, i, j] = H2 + Hl[i] - H3 - H1[i]
+    t_plain = time.perf_counter() - t0
+    net = learned.BandwidthMLP.load(ctx)
+    learned.hestimate_learned(ctx, net, list(x), skip_levels=6)  # warm-up
+    ctx.te_all_pairs(x, hp, list(taus))
+    sync()
+    t0 = time.perf_counter()
+    hl, st = learned.hestimate_learned(ctx, net, list(x), skip_levels=6)
+    te_b = ctx.te_all_pairs(x, hl[:, 0], list(taus))
+    t_b = time.perf_counter() - t0
+    off = ~np.eye(M, dtype=bool)
+    return {"workload": f"AMISE bandwidths for {M} columns, then TE of all {M * (M - 1)} ordered "
+                        f"pairs at lags {list(taus)} ({M} x {N} Langevin)",
+            "plain_s": t_plain, "plain_density_calls": calls, "batched_learned_s": t_b,
+            "speedup": t_plain / t_b, "te_estimates": int(len(taus) * M * (M - 1)),
+            "bandwidths_identical": bool(np.array_equal(hl[:, 0], hp)),
+            "max_abs_dTE_batched_vs_plain": float(np.max(np.abs(te_b - te_plain)[:, off])),
+            "learned_fallbacks": int(sum(1 - s[0]["warm_converged"] for s in st))}
+
+
 def other_configs(ctx):
     """The other configurations, measured once (device time of one call each):
     config 1 (1-D GMM density), config 3 (TE, all ordered pairs, 3 lags) and
@@ -481,6 +539,11 @@ def main():
             line["batched_learned_vs_plain"] = compare_plain(ctx, x, ptr)
         except Exception as exc:
             line["batched_learned_vs_plain"] = {"error": str(exc)[:300]}
+    if not args.no_compare and ws == 1:
+        try:
+            line["te_batched_learned_vs_plain"] = compare_plain_te(ctx)
+        except Exception as exc:
+            line["te_batched_learned_vs_plain"] = {"error": str(exc)[:300]}
     if not args.no_extra and ws == 1:
         try:
             line["other_configs"] = other_configs(ctx)
