@@ -57,6 +57,9 @@ SIGNATURES: dict[str, tuple] = {
     "ent_set_tuning": (C.c_int, [C.c_void_p, C.c_void_p]),
     "ent_log64_selftest": (C.c_int, [C.c_void_p, c_f64_p, C.c_size_t, c_f64_p]),
     "ent_wait_selftest": (C.c_int, [C.c_void_p]),
+    "ent_autotune": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_uint32, C.c_uint32,
+                               C.c_void_p]),
+    "ent_autotune_cache_size": (C.c_size_t, [C.c_void_p]),
     "ent_get_tuning": (C.c_int, [C.c_void_p, C.c_void_p]),
     "ent_densities": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, c_u32_p, c_f32_p,
                                 c_u32_p, C.c_uint32, C.c_uint32, C.c_void_p, c_size_p]),

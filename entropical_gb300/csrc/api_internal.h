@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <map>
 #include <string>
 #include <vector>
 
@@ -41,6 +42,13 @@ struct Ctx {
   bool pending_pairs = false;
   uint32_t strip_subdiv = 2;  // cells per bandwidth along dimension 1 (d = 2)
   uint32_t strip_subdiv3 = 1;  // cells per bandwidth along dimensions 1, 2 (d = 3)
+  // autotune cache: (d << 8 | size bucket) -> {pair body, targets per warp,
+  // cells per bandwidth}
+  struct TuneChoice {
+    int variant, tile_r;
+    uint32_t cells;
+  };
+  std::map<uint32_t, TuneChoice> tune_cache;
   int tile_r[3] = {16, 16, 8};  // targets per warp of the pair kernel, by d
   // pair body per dimension: 0 min-based, 1 saturating FMA, 2 saturating at
   // 5 CTAs/SM, 3 as 2 with larger chunks (fastest measured: 2, 2, 1)

@@ -292,3 +292,88 @@ int ent_entropy_batch(ent_ctx* ctx, const ent_instance* inst, size_t n_inst,
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------ autotuner
+namespace {
+
+struct TuneCand {
+  int variant, tile_r;
+  uint32_t cells;
+};
+
+// Candidate shapes per density dimension: pair body (ent_tuning numbering
+// minus one), targets per warp of the ordered bodies, cells per bandwidth
+// (dimension 1 for d = 2, dimensions 1 and 2 for d = 3).
+std::vector<TuneCand> tune_candidates(uint32_t d) {
+  if (d == 1) return {{2, 16, 2}, {4, 16, 2}, {5, 16, 2}};
+  if (d == 2) return {{2, 16, 2}, {4, 16, 1}, {4, 16, 2}, {4, 16, 3}, {5, 16, 2}};
+  return {{1, 8, 1}, {2, 8, 1}, {4, 8, 1}, {4, 8, 2}, {5, 8, 1}};
+}
+
+void apply_choice(Ctx& c, uint32_t d, int variant, int tile_r, uint32_t cells) {
+  c.pair_variant[d - 1] = variant;
+  c.tile_r[d - 1] = tile_r;
+  if (d == 2) c.strip_subdiv = cells;
+  if (d == 3) c.strip_subdiv3 = cells;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ent_autotune(ent_ctx* ctx, const ent_instance* sample, size_t n_sample, uint32_t d,
+                 uint32_t flags, ent_tuning* chosen) {
+  if (!ctx) return ENT_ERR_ARG;
+  Ctx& c = *reinterpret_cast<Ctx*>(ctx);
+  if (d < 1 || d > 3) return c.fail(ENT_ERR_DIM, ent_status_string(ENT_ERR_DIM));
+  if (!sample || n_sample == 0) return c.fail(ENT_ERR_ARG, "empty sample");
+  uint64_t nmax = 0;
+  for (size_t q = 0; q < n_sample; ++q)
+    if (sample[q].d == d) nmax = std::max<uint64_t>(nmax, sample[q].n);
+  if (nmax == 0) return c.fail(ENT_ERR_ARG, "no sample instance of dimension d");
+  int bucket = 0;
+  while ((2ull << bucket) <= nmax) ++bucket;
+  const uint32_t key = (d << 8) | (uint32_t)bucket;
+  auto it = c.tune_cache.find(key);
+  if (it != c.tune_cache.end() && !(flags & ENT_TUNE_FORCE)) {
+    apply_choice(c, d, it->second.variant, it->second.tile_r, it->second.cells);
+  } else {
+    const Ctx::TuneChoice keep{c.pair_variant[d - 1], c.tile_r[d - 1],
+                               d == 2 ? c.strip_subdiv : c.strip_subdiv3};
+    std::vector<double> h(n_sample);
+    const uint32_t bflags = flags & ENT_BATCH_DEVICE_INPUT;
+    float best = 0.f;
+    Ctx::TuneChoice pick = keep;
+    bool have = false;
+    for (const TuneCand& t : tune_candidates(d)) {
+      apply_choice(c, d, t.variant, t.tile_r, t.cells);
+      float ms = 0.f;
+      for (int rep = 0; rep < 3; ++rep) {  // first run warms up
+        const int s = ent_entropy_batch(ctx, sample, n_sample, bflags, h.data());
+        if (s) {
+          apply_choice(c, d, keep.variant, keep.tile_r, keep.cells);
+          return s;
+        }
+        const float m = c.stats.pair_kernel_ms_by_dim[d - 1];
+        if (rep == 1 || (rep == 2 && m < ms)) ms = m;
+      }
+      if (!have || ms < best) {
+        best = ms;
+        pick = {t.variant, t.tile_r, t.cells};
+        have = true;
+      }
+    }
+    c.tune_cache[key] = pick;
+    apply_choice(c, d, pick.variant, pick.tile_r, pick.cells);
+  }
+  if (chosen) return ent_get_tuning(ctx, chosen);
+  return ENT_OK;
+}
+
+size_t ent_autotune_cache_size(const ent_ctx* ctx) {
+  if (!ctx) return 0;
+  return reinterpret_cast<const Ctx*>(ctx)->tune_cache.size();
+}
+
+}  // extern "C"
+

@@ -281,6 +281,40 @@ class Context:
             out.ctypes.data_as(c_f64_p)))
         return out
 
+    def _instances(self, instances, device: bool):
+        arr = (Instance * len(instances))()
+        keep = []
+        for q, item in enumerate(instances):
+            if device:
+                addr, d, n, h = item
+                arr[q].coords = C.c_void_p(addr)
+            else:
+                x, h = item
+                x = np.ascontiguousarray(np.atleast_2d(x), dtype=np.float32)
+                keep.append(x)
+                d, n = x.shape
+                arr[q].coords = x.ctypes.data_as(C.c_void_p)
+            arr[q].n = n
+            arr[q].d = d
+            for j in range(d):
+                arr[q].h[j] = float(h[j])
+        return arr, keep
+
+    def autotune(self, instances, d: int, force: bool = False, device: bool = False) -> dict:
+        """The library's own autotuner (ent_autotune): time the candidate shapes of
+        dimension d on a sample batch [(coords (d, n), h)...] (or device tuples
+        as in entropy_batch), apply the fastest and keep it in the context's
+        cache; returns the context's tuning afterwards."""
+        arr, keep = self._instances(instances, device)
+        t = _native.Tuning()
+        flags = (1 if force else 0) | (BATCH_DEVICE_INPUT if device else 0)
+        self.check(self._lib.ent_autotune(self._h, C.cast(arr, C.c_void_p), len(instances),
+                                          int(d), flags, C.byref(t)))
+        return self.tuning()
+
+    def autotune_cache_size(self) -> int:
+        return int(self._lib.ent_autotune_cache_size(self._h))
+
     def entropy_batch(self, instances, counts: bool = False, device: bool = False) -> np.ndarray:
         """Resubstitution entropies of [(coords (d, n), h (d,))...] in one batch.
         With device=True, coords entries are raw device addresses and the

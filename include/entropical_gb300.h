@@ -203,6 +203,27 @@ typedef struct {
 int ent_entropy_batch(ent_ctx* ctx, const ent_instance* inst, size_t n_inst,
                       uint32_t flags, double* h_out);
 
+/* ------------------------------------------------------------ autotuner */
+
+#define ENT_TUNE_FORCE 1u /* re-time even if the cache holds the bucket */
+
+/*
+ * Autotuner of the pair kernel's tile shapes. Times every candidate pair
+ * body and cell size for density dimension d (1..3) on the sample batch
+ * (ent_entropy_batch with ENT_BATCH_DEVICE_INPUT in flags if the sample is
+ * in device memory; device time of that dimension's pair kernel, best of 2)
+ * and applies the fastest to the context, as ent_set_tuning would. The
+ * choice is kept in the context's cache under (d, floor(log2 of the largest
+ * sample instance of dimension d)); a later call for the same key applies the
+ * cached choice without timing (unless ENT_TUNE_FORCE). chosen (nullable)
+ * receives the context's tuning afterwards. The sample must contain an
+ * instance of dimension d. No counterpart in the reference.
+ */
+int ent_autotune(ent_ctx* ctx, const ent_instance* sample, size_t n_sample,
+                 uint32_t d, uint32_t flags, ent_tuning* chosen);
+/* Number of entries in the context's autotune cache. */
+size_t ent_autotune_cache_size(const ent_ctx* ctx);
+
 /* ------------------------------------------------------ coordinate files */
 
 /*

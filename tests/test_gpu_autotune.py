@@ -25,3 +25,28 @@ def test_tune_and_apply(tmp_path, monkeypatch):
     with Context(0) as ctx2:
         assert autotune.apply(ctx2, 2, x.shape[1])
         assert ctx2.tuning()["pair_variant_by_dim"][1] == choice["pair_variant"]
+
+
+def test_native_autotuner_cache():
+    """ent_autotune: the context's own tuner picks a shape per dimension on a
+    sample batch, caches it per (d, size bucket), and results stay the same."""
+    from entropical_gb300 import Context
+    rng = np.random.default_rng(8)
+    sample = []
+    for d in (1, 2, 3):
+        for n in (3000, 7000):
+            x = workloads.mixture_instance(rng, d, n)
+            sample.append((x, workloads.scott_bandwidth(x, d)))
+    with Context(0) as ctx:
+        ref = ctx.entropy_batch(sample)
+        picks = {}
+        for d in (1, 2, 3):
+            t = ctx.autotune(sample, d)
+            assert 0 <= t["pair_variant_by_dim"][d - 1] <= 5
+            picks[d] = (t["pair_variant_by_dim"][d - 1], t["cells_per_h"], t["cells_per_h3"])
+        assert ctx.autotune_cache_size() == 3
+        ctx.set_tuning(pair_variant=0, cells_per_h=4, cells_per_h3=2)
+        t2 = ctx.autotune(sample, 2)  # cached: applied again without timing
+        assert t2["pair_variant_by_dim"][1] == picks[2][0] and t2["cells_per_h"] == picks[2][1]
+        assert ctx.autotune_cache_size() == 3
+        assert np.allclose(ctx.entropy_batch(sample), ref, rtol=0, atol=2e-6)
