@@ -103,3 +103,8 @@ epa_convolution(const std::vector<float>& sorted_coords
   if (s != ENT_OK) fail(c, s);
   return out;
 }
+
+ent_ctx* densities_gb300_context() {
+  std::lock_guard<std::mutex> lock(g_mu);
+  return context();
+}

@@ -32,3 +32,10 @@ combined_densities(const float* coords
 float
 epa_convolution(const std::vector<float>& sorted_coords
               , float h);
+
+// Not in the reference interface: the shim's own context (created on first
+// use), for callers that want the C ABI's extras on it, e.g. ent_autotune or
+// ent_set_tuning before the estimators run. Guarded by the shim's lock only
+// inside the three functions above; do not use it concurrently with them.
+typedef struct ent_ctx ent_ctx;
+ent_ctx* densities_gb300_context();
