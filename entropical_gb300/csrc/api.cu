@@ -318,7 +318,9 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
       }
       I.perm0 = vvals + voff[s.view[0]];
       I.S = s.d == 2 ? std::max(1u, std::min(4u, s.S))
-                     : (s.d == 3 ? std::max(1u, std::min(2u, c.strip_subdiv3)) : 1u);
+                     : (s.d == 3 ? std::max(1u, std::min(2u, s.S3[0] ? s.S3[0] : c.strip_subdiv3))
+                                 : 1u);
+      I.S2 = s.d == 3 ? std::max(1u, std::min(2u, s.S3[1] ? s.S3[1] : c.strip_subdiv3)) : 1u;
       I.ncell1 = I.ncell2 = 1;
       if (s.d >= 2) {
         const ViewStats& a = vs[s.view[1]];
@@ -333,7 +335,7 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
       }
       if (s.d == 3) {
         const ViewStats& b = vs[s.view[2]];
-        const double w = (double)s.h[2] / I.S * (1.0 + 1e-4);
+        const double w = (double)s.h[2] / I.S2 * (1.0 + 1e-4);
         I.lo2 = b.mn;
         I.inv_w2 = 1.0 / w;
         I.ncell2 = (uint32_t)std::min<double>(

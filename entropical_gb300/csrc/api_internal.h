@@ -79,6 +79,8 @@ struct InstSpec {
   double norm = 1.0;
   double* out = nullptr;  // device, by original index (nullable)
   uint32_t S = 2;
+  // d = 3: cells per bandwidth along dimensions 1 and 2 (0: the context's)
+  uint32_t S3[2] = {0, 0};
 };
 
 namespace ent { struct ViewStats; }

@@ -312,10 +312,10 @@ __global__ void k_plan(const InstDev* __restrict__ insts, uint32_t n_inst,
     for (int c = max(0, c1 - S); c <= min((int)I.ncell1 - 1, c1 + S); ++c)
       add_strip((uint32_t)c);
   } else {
-    const int S = (int)I.S;
+    const int S = (int)I.S, S2 = (int)I.S2;
     const int c1 = (int)(s / I.ncell2), c2 = (int)(s % I.ncell2);
     for (int u = max(0, c1 - S); u <= min((int)I.ncell1 - 1, c1 + S); ++u)
-      for (int v = max(0, c2 - S); v <= min((int)I.ncell2 - 1, c2 + S); ++v)
+      for (int v = max(0, c2 - S2); v <= min((int)I.ncell2 - 1, c2 + S2); ++v)
         add_strip((uint32_t)u * I.ncell2 + (uint32_t)v);
   }
   td.n_runs = nr;

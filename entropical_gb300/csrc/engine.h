@@ -66,6 +66,8 @@ struct InstDev {
   double* out;              // per-point density by original index (nullable)
   uint32_t tt;              // targets per tile
   uint32_t sym;             // 1: symmetric evaluation (each unordered pair once)
+  uint32_t S2;              // d = 3: cells per bandwidth along dimension 2
+  uint32_t pad2;
   double* acc;              // symmetric mode: unscaled sums by sorted position
 };
 

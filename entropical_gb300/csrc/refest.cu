@@ -166,7 +166,9 @@ struct Batch {
     vt.n_rows = n_rows;
   }
   // density of d lagged columns, normalised by n_rows; returns its index
-  uint32_t add(uint32_t d, const size_t* cols, const uint32_t* lags, const float* h) {
+  // s3: d = 3 cells per bandwidth along dimensions 1 and 2 (0: the context's)
+  uint32_t add(uint32_t d, const size_t* cols, const uint32_t* lags, const float* h,
+               uint32_t s3a = 0, uint32_t s3b = 0) {
     uint32_t mx = 0;
     for (uint32_t j = 0; j < d; ++j) mx = std::max(mx, lags[j]);
     const uint32_t n = (uint32_t)(vt.n_rows - mx);
@@ -179,6 +181,8 @@ struct Batch {
     }
     I.norm = (double)vt.n_rows;
     I.S = c.strip_subdiv;
+    I.S3[0] = s3a;
+    I.S3[1] = s3b;
     insts.push_back(I);
     out_off.push_back(total);
     total += n;
@@ -352,11 +356,13 @@ int ent_reference_estimator(ent_ctx* ctx, const float* coords, size_t n_rows, si
           const size_t ca[3] = {i, i, j};
           const uint32_t la[3] = {0, tau, 0};
           const float ha[3] = {h[i], h[i], h[j]};
-          p3a[i * M + j] = B.add(3, ca, la, ha);  // p_ij_itau
+          // (x_i, x_i+tau, x_j): dimension 1 follows the sorted dimension 0
+          p3a[i * M + j] = B.add(3, ca, la, ha, 1, 2);  // p_ij_itau
           const size_t cb[3] = {i, j, j};
           const uint32_t lb[3] = {0, 0, tau};
           const float hb[3] = {h[i], h[j], h[j]};
-          p3b[i * M + j] = B.add(3, cb, lb, hb);  // p_ij_jtau
+          // (x_i, x_j, x_j+tau): dimension 2 follows dimension 1
+          p3b[i * M + j] = B.add(3, cb, lb, hb, 2, 1);  // p_ij_jtau
         }
       }
   if ((s = B.run())) return s;
