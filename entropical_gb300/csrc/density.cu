@@ -43,11 +43,9 @@ constexpr unsigned FULL = 0xffffffffu;
 __global__ void __launch_bounds__(1024)
     k_colstats(const ViewDev* __restrict__ views, ViewStats* __restrict__ stats) {
   __shared__ float smn[32], smx[32];
-  __shared__ double ss1[32], ss2[32];
   __shared__ uint32_t sbad[32];
   const ViewDev v = views[blockIdx.x];
   float mn = FLT_MAX, mx = -FLT_MAX;
-  double s1 = 0.0, s2 = 0.0;
   uint32_t bad = 0;
   for (uint32_t i = threadIdx.x; i < v.n; i += blockDim.x) {
     const float f = v.x[i];
@@ -57,22 +55,16 @@ __global__ void __launch_bounds__(1024)
     }
     mn = fminf(mn, f);
     mx = fmaxf(mx, f);
-    s1 += (double)f;
-    s2 += (double)f * (double)f;
   }
   for (int o = 16; o; o >>= 1) {
     mn = fminf(mn, __shfl_xor_sync(FULL, mn, o));
     mx = fmaxf(mx, __shfl_xor_sync(FULL, mx, o));
-    s1 += __shfl_xor_sync(FULL, s1, o);
-    s2 += __shfl_xor_sync(FULL, s2, o);
     bad |= __shfl_xor_sync(FULL, bad, o);
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (lane == 0) {
     smn[warp] = mn;
     smx[warp] = mx;
-    ss1[warp] = s1;
-    ss2[warp] = s2;
     sbad[warp] = bad;
   }
   __syncthreads();
@@ -80,22 +72,16 @@ __global__ void __launch_bounds__(1024)
     const int nw = blockDim.x >> 5;
     mn = lane < nw ? smn[lane] : FLT_MAX;
     mx = lane < nw ? smx[lane] : -FLT_MAX;
-    s1 = lane < nw ? ss1[lane] : 0.0;
-    s2 = lane < nw ? ss2[lane] : 0.0;
     bad = lane < nw ? sbad[lane] : 0u;
     for (int o = 16; o; o >>= 1) {
       mn = fminf(mn, __shfl_xor_sync(FULL, mn, o));
       mx = fmaxf(mx, __shfl_xor_sync(FULL, mx, o));
-      s1 += __shfl_xor_sync(FULL, s1, o);
-      s2 += __shfl_xor_sync(FULL, s2, o);
       bad |= __shfl_xor_sync(FULL, bad, o);
     }
     if (lane == 0) {
       ViewStats r;
       r.mn = mn;
       r.mx = mx;
-      r.s1 = s1;
-      r.s2 = s2;
       r.nonfinite = bad;
       r.pad = 0;
       stats[blockIdx.x] = r;

@@ -41,7 +41,6 @@ struct ViewDev {
 
 struct ViewStats {
   float mn, mx;
-  double s1, s2;  // sum and sum of squares (FP64)
   uint32_t nonfinite;
   uint32_t pad;
 };

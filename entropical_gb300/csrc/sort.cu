@@ -84,13 +84,19 @@ __global__ void __launch_bounds__(1024) k_radix_scan(SegTableDev t) {
   }
 }
 
+// Stable scatter of one block's chunk: every element's rank among the
+// chunk's elements of its digit is found with warp matches and per-warp
+// digit counts (in element order), the chunk is reordered by digit in shared
+// memory, and the digit runs are written out contiguously (coalesced).
 __global__ void __launch_bounds__(RS_THREADS)
     k_radix_scatter(const uint32_t* __restrict__ kin,
                     const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
                     uint32_t* __restrict__ vout, int shift, SegTableDev t) {
-  __shared__ uint32_t off[256];
+  __shared__ uint32_t off[256];    // global start of each digit for this block
+  __shared__ uint32_t lstart[256]; // start of each digit in the block's chunk
   __shared__ uint32_t run[256];
   __shared__ uint32_t wcnt[RS_WARPS][256];
+  __shared__ uint32_t sk[RS_CHUNK], sv[RS_CHUNK];
   const uint32_t b = blockIdx.x;
   const uint32_t s = t.blk_seg[b];
   const uint32_t j = b - t.seg_blk0[s];
@@ -98,9 +104,31 @@ __global__ void __launch_bounds__(RS_THREADS)
   const uint64_t base = t.seg_off[s];
   const uint32_t len = t.seg_len[s];
   const uint32_t e0 = j * RS_CHUNK;
+  const uint32_t ne = min((uint32_t)RS_CHUNK, len - e0);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   off[threadIdx.x] =
       t.hist[(uint64_t)t.seg_blk0[s] * 256 + (uint64_t)threadIdx.x * nb + j];
+  // digit counts of the chunk -> local digit starts (exclusive scan)
+  run[threadIdx.x] = 0;
+  __syncthreads();
+  for (uint32_t e = threadIdx.x; e < ne; e += RS_THREADS)
+    atomicAdd(&run[(kin[base + e0 + e] >> shift) & 255u], 1u);
+  __syncthreads();
+  {
+    const uint32_t c = run[threadIdx.x];
+    uint32_t x = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) wcnt[0][warp] = x;
+    __syncthreads();
+    uint32_t wp = 0;
+    for (int w = 0; w < warp; ++w) wp += wcnt[0][w];
+    lstart[threadIdx.x] = wp + x - c;
+    __syncthreads();
+  }
   run[threadIdx.x] = 0;
   const uint32_t lt_mask = (1u << lane) - 1u;
   for (int it = 0; it < RS_ITEMS; ++it) {
@@ -131,11 +159,20 @@ __global__ void __launch_bounds__(RS_THREADS)
     }
     __syncthreads();
     if (valid) {
-      const uint32_t pos = off[digit] + wcnt[warp][digit] + rank;
-      kout[base + pos] = key;
-      vout[base + pos] = val;
+      const uint32_t lp = lstart[digit] + wcnt[warp][digit] + rank;
+      sk[lp] = key;
+      sv[lp] = val;
     }
     __syncthreads();
+  }
+  // chunk in digit order: consecutive elements of a digit go to consecutive
+  // global positions
+  for (uint32_t i = threadIdx.x; i < ne; i += RS_THREADS) {
+    const uint32_t key = sk[i];
+    const uint32_t d = (key >> shift) & 255u;
+    const uint32_t pos = off[d] + (i - lstart[d]);
+    kout[base + pos] = key;
+    vout[base + pos] = sv[i];
   }
 }
 
