@@ -84,18 +84,21 @@ __global__ void __launch_bounds__(1024) k_radix_scan(SegTableDev t) {
   }
 }
 
-// Stable scatter of one block's chunk: every element's rank among the
-// chunk's elements of its digit is found with warp matches and per-warp
-// digit counts (in element order), the chunk is reordered by digit in shared
-// memory, and the digit runs are written out contiguously (coalesced).
+// Stable scatter of one block's chunk (RS_CHUNK elements; warp w owns the
+// RS_ITEMS * 32 consecutive elements from w * RS_ITEMS * 32). Each warp ranks
+// its elements per digit with warp matches and warp-private digit counts (in
+// element order); one block-wide scan over (digit, warp) turns the counts
+// into positions in the chunk sorted by digit; the chunk is reordered in
+// shared memory and its digit runs are written out contiguously (coalesced).
+// Four block barriers per chunk.
 __global__ void __launch_bounds__(RS_THREADS)
     k_radix_scatter(const uint32_t* __restrict__ kin,
                     const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
                     uint32_t* __restrict__ vout, int shift, SegTableDev t) {
-  __shared__ uint32_t off[256];    // global start of each digit for this block
-  __shared__ uint32_t lstart[256]; // start of each digit in the block's chunk
-  __shared__ uint32_t run[256];
+  __shared__ uint32_t off[256];     // global start of each digit for this block
+  __shared__ uint32_t lstart[256];  // start of each digit in the reordered chunk
   __shared__ uint32_t wcnt[RS_WARPS][256];
+  __shared__ uint32_t wtot[RS_WARPS];
   __shared__ uint32_t sk[RS_CHUNK], sv[RS_CHUNK];
   const uint32_t b = blockIdx.x;
   const uint32_t s = t.blk_seg[b];
@@ -108,70 +111,76 @@ __global__ void __launch_bounds__(RS_THREADS)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   off[threadIdx.x] =
       t.hist[(uint64_t)t.seg_blk0[s] * 256 + (uint64_t)threadIdx.x * nb + j];
-  // digit counts of the chunk -> local digit starts (exclusive scan)
-  run[threadIdx.x] = 0;
-  __syncthreads();
-  for (uint32_t e = threadIdx.x; e < ne; e += RS_THREADS)
-    atomicAdd(&run[(kin[base + e0 + e] >> shift) & 255u], 1u);
-  __syncthreads();
-  {
-    const uint32_t c = run[threadIdx.x];
-    uint32_t x = c;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += y;
-    }
-    if (lane == 31) wcnt[0][warp] = x;
-    __syncthreads();
-    uint32_t wp = 0;
-    for (int w = 0; w < warp; ++w) wp += wcnt[0][w];
-    lstart[threadIdx.x] = wp + x - c;
-    __syncthreads();
-  }
-  run[threadIdx.x] = 0;
+  for (int w = 0; w < RS_WARPS; ++w) wcnt[w][threadIdx.x] = 0;
+  __syncthreads();
+  // 1. per warp: rank of every element among the warp's elements of its digit
   const uint32_t lt_mask = (1u << lane) - 1u;
-  for (int it = 0; it < RS_ITEMS; ++it) {
+  uint32_t key[RS_ITEMS], val[RS_ITEMS], rnk[RS_ITEMS];
+  uint32_t* myc = wcnt[warp];
 #pragma unroll
-    for (int w = 0; w < RS_WARPS; ++w) wcnt[w][threadIdx.x] = 0;
-    __syncthreads();
-    const uint32_t e = e0 + it * RS_THREADS + threadIdx.x;
-    const bool valid = e < len;
-    uint32_t key = 0, val = 0, digit = 256;
+  for (int it = 0; it < RS_ITEMS; ++it) {
+    const uint32_t e = (uint32_t)warp * (RS_ITEMS * 32) + it * 32 + lane;
+    const bool valid = e < ne;
+    uint32_t digit = 256;
+    key[it] = 0;
+    val[it] = 0;
     if (valid) {
-      key = kin[base + e];
-      val = vin[base + e];
-      digit = (key >> shift) & 255u;
+      key[it] = kin[base + e0 + e];
+      val[it] = vin[base + e0 + e];
+      digit = (key[it] >> shift) & 255u;
     }
     const uint32_t peers = __match_any_sync(0xffffffffu, digit);
-    const uint32_t rank = __popc(peers & lt_mask);
-    if (valid && rank == 0) wcnt[warp][digit] = __popc(peers);
-    __syncthreads();
-    {  // exclusive scan over warps, per digit, continuing the running count
-      uint32_t r = run[threadIdx.x];
-#pragma unroll
-      for (int w = 0; w < RS_WARPS; ++w) {
-        const uint32_t c = wcnt[w][threadIdx.x];
-        wcnt[w][threadIdx.x] = r;
-        r += c;
-      }
-      run[threadIdx.x] = r;
-    }
-    __syncthreads();
-    if (valid) {
-      const uint32_t lp = lstart[digit] + wcnt[warp][digit] + rank;
-      sk[lp] = key;
-      sv[lp] = val;
-    }
-    __syncthreads();
+    const uint32_t r = __popc(peers & lt_mask);
+    const uint32_t prior = valid ? myc[digit] : 0u;
+    __syncwarp();
+    if (valid && r == 0) myc[digit] = prior + __popc(peers);
+    __syncwarp();
+    rnk[it] = prior + r;
   }
-  // chunk in digit order: consecutive elements of a digit go to consecutive
-  // global positions
+  __syncthreads();
+  // 2. thread d: digit d's total and per-warp starts; block scan over digits
+  const uint32_t d = threadIdx.x;
+  uint32_t tot = 0;
+#pragma unroll
+  for (int w = 0; w < RS_WARPS; ++w) {
+    const uint32_t c = wcnt[w][d];
+    wcnt[w][d] = tot;
+    tot += c;
+  }
+  uint32_t x = tot;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) wtot[warp] = x;
+  __syncthreads();
+  uint32_t wp = 0;
+  for (int w = 0; w < warp; ++w) wp += wtot[w];
+  const uint32_t start = wp + x - tot;
+  lstart[d] = start;
+#pragma unroll
+  for (int w = 0; w < RS_WARPS; ++w) wcnt[w][d] += start;
+  __syncthreads();
+  // 3. reorder the chunk by digit in shared memory
+#pragma unroll
+  for (int it = 0; it < RS_ITEMS; ++it) {
+    const uint32_t e = (uint32_t)warp * (RS_ITEMS * 32) + it * 32 + lane;
+    if (e < ne) {
+      const uint32_t dg = (key[it] >> shift) & 255u;
+      const uint32_t lp = myc[dg] + rnk[it];
+      sk[lp] = key[it];
+      sv[lp] = val[it];
+    }
+  }
+  __syncthreads();
+  // 4. digit runs to their global positions, consecutive elements together
   for (uint32_t i = threadIdx.x; i < ne; i += RS_THREADS) {
-    const uint32_t key = sk[i];
-    const uint32_t d = (key >> shift) & 255u;
-    const uint32_t pos = off[d] + (i - lstart[d]);
-    kout[base + pos] = key;
+    const uint32_t k = sk[i];
+    const uint32_t dg = (k >> shift) & 255u;
+    const uint32_t pos = off[dg] + (i - lstart[dg]);
+    kout[base + pos] = k;
     vout[base + pos] = sv[i];
   }
 }
