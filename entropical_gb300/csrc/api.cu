@@ -345,13 +345,30 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
       max_strips = std::max(max_strips, I.n_strips);
       I.tt = (uint32_t)(sym_d[d] ? sym_tile_targets(d, var_d[d])
                                  : density_tile_targets((int)s.d, c.tile_r[s.d - 1]));
-      I.tile_cap = (s.n + I.tt - 1) / I.tt + std::min(I.n_strips, s.n);
-      I.tile_base = slot;
-      slot += I.tile_cap;
+      I.tile_cap = (s.n + I.tt - 1) / I.tt + std::min(I.n_strips, s.n);  // tiles
       I.scale = (mode & DM_COUNT) ? 1.0 : std::pow(0.75, (double)s.d) / (s.norm * prod_hg2);
       I.out = s.out;
       I.sym = sym_d[d] ? 1u : 0u;
       if (I.sym) sym_points += s.n;
+    }
+    // Work items: a batch with few tiles for the persistent grid (a single
+    // density, say) splits every tile's sources into up to 8 shares so that
+    // all CTAs get work; only the symmetric kernel adds its target sums
+    // atomically and can take shares.
+    uint64_t tiles_d = 0;
+    for (uint32_t i : order)
+      if ((int)insts[i].d == d) tiles_d += hi[i].tile_cap;
+    uint32_t parts = 1;
+    const uint64_t want = 16ull * (uint64_t)c.n_sms;
+    if (sym_d[d] && tiles_d > 0 && tiles_d < want)
+      parts = (uint32_t)std::min<uint64_t>(8, (want + tiles_d - 1) / tiles_d);
+    for (uint32_t i : order) {
+      if ((int)insts[i].d != d) continue;
+      InstDev& I = hi[i];
+      I.parts = parts;
+      I.tile_cap *= parts;
+      I.tile_base = slot;
+      slot += I.tile_cap;
     }
     group_slots[d] = slot - group_base[d];
   }

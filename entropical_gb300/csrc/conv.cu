@@ -162,6 +162,8 @@ __global__ void k_conv_plan(const ConvCol* __restrict__ cols, uint32_t n_cols,
   td.n_runs = 0;
   td.t_count = 0;
   td.t_begin = 0;
+  td.part = 0;
+  td.pad = 0;
   const uint32_t t = g - C.tile_base;
   if (t < C.n_tiles) {
     const uint32_t tb = t * tt;

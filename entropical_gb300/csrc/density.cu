@@ -245,7 +245,11 @@ __global__ void k_plan(const InstDev* __restrict__ insts, uint32_t n_inst,
   td.t_begin = 0;
   td.t_count = 0;
   td.n_runs = 0;
-  const uint32_t t = g - I.tile_base;
+  td.pad = 0;
+  // slot -> (tile, share of its sources)
+  const uint32_t parts = max(I.parts, 1u);
+  const uint32_t t = (g - I.tile_base) / parts;
+  td.part = (g - I.tile_base) % parts;
   const uint32_t total = I.tile_off[I.n_strips];
   if (t >= total) {
     tiles[g] = td;
@@ -305,6 +309,25 @@ __global__ void k_plan(const InstDev* __restrict__ insts, uint32_t n_inst,
         add_strip((uint32_t)u * I.ncell2 + (uint32_t)v);
   }
   td.n_runs = nr;
+  if (parts > 1) {
+    // this slot's share [a, b) of the concatenated source runs (symmetric
+    // kernel only: its target sums are atomic, so shares may run anywhere)
+    const unsigned long long a = nsrc * td.part / parts, b = nsrc * (td.part + 1) / parts;
+    unsigned long long pre = 0;
+    uint32_t n2 = 0;
+    for (uint32_t r = 0; r < nr; ++r) {
+      const uint32_t rlo = td.lo[r], rlen = td.len[r];  // before n2 <= r overwrites
+      const unsigned long long s0 = max(a, pre), s1 = min(b, pre + rlen);
+      if (s1 > s0) {
+        td.lo[n2] = rlo + (uint32_t)(s0 - pre);
+        td.len[n2] = (uint32_t)(s1 - s0);
+        ++n2;
+      }
+      pre += rlen;
+    }
+    td.n_runs = n2;
+    nsrc = b - a;
+  }
   tiles[g] = td;
   if (n_src_total) atomicAdd(n_src_total + (d - 1), nsrc * (unsigned long long)tc);
 }

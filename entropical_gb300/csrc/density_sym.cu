@@ -288,7 +288,7 @@ __global__ void __launch_bounds__(256)
   const int lane = threadIdx.x & 31;
   if (g >= n_slots) return;  // warp-uniform
   const TileDesc& T = tiles[g];
-  const uint32_t tc = T.t_count;
+  const uint32_t tc = T.part == 0 ? T.t_count : 0u;  // one slot per tile finishes it
   double ls = 0.0;
   if (tc) {
     const InstDev& I = insts[T.inst];

@@ -66,7 +66,8 @@ struct InstDev {
   uint32_t tt;              // targets per tile
   uint32_t sym;             // 1: symmetric evaluation (each unordered pair once)
   uint32_t S2;              // d = 3: cells per bandwidth along dimension 2
-  uint32_t pad2;
+  uint32_t parts;           // work items per tile (source runs split; 0 = 1);
+                            // tile_cap counts work-item slots
   double* acc;              // symmetric mode: unscaled sums by sorted position
 };
 
@@ -75,6 +76,8 @@ struct TileDesc {
   uint32_t t_begin;  // first target (position in the sorted order)
   uint32_t t_count;  // 0 marks an unused slot
   uint32_t n_runs;
+  uint32_t part;     // which share of the tile's sources (symmetric kernel)
+  uint32_t pad;
   uint32_t lo[MAX_RUNS];   // candidate-source runs (sorted positions)
   uint32_t len[MAX_RUNS];
 };

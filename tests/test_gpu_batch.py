@@ -1,6 +1,8 @@
 """GPU parity of the batched estimators (one persistent launch for all
 instances) against the plain per-instance path and the FP64 oracle.
-Entropies and MI: 1e-6 nats absolute against the FP64 oracle."""
+Entropies and MI: 1e-6 nats absolute against the FP64 oracle; batch vs plain
+calls 1e-7 (a small batch splits each tile's sources into a different number
+of work items, which changes the FP32 partial sums, not the terms)."""
 import numpy as np
 import pytest
 
@@ -29,10 +31,10 @@ def test_mi_all_pairs_matches_plain_path(ctx):
     mi, hx = ctx.mi_all_pairs(x, h)
     for i in range(5):
         p = ctx.combined_densities(x, None, [i], [h[i]])
-        assert abs(hx[i] + np.mean(np.log(p))) < 1e-9
+        assert abs(hx[i] + np.mean(np.log(p))) < 1e-7
     for i, j in [(0, 4), (1, 3)]:
         pij = ctx.combined_densities(x, None, [i, j], [h[i], h[j]])
-        assert abs(mi[i, j] - (hx[i] + hx[j] + np.mean(np.log(pij)))) < 1e-9
+        assert abs(mi[i, j] - (hx[i] + hx[j] + np.mean(np.log(pij)))) < 1e-7
 
 
 def test_support_counts_batch(ctx):
@@ -60,7 +62,7 @@ def test_uneven_batch(ctx):
     for q in range(1, 24, 5):
         x, h = insts[q]
         p = ctx.combined_densities(x, None, list(range(x.shape[0])), h)
-        assert abs(H[q] + np.mean(np.log(p))) < 1e-9
+        assert abs(H[q] + np.mean(np.log(p))) < 1e-7
 
 
 def test_te_all_pairs_matches_oracle(ctx):
