@@ -34,8 +34,8 @@ struct ConvCol {
   const float* xs;  // value-sorted column (n + 8 floats)
   uint32_t n;
   uint32_t tile_base;
-  uint32_t n_tiles;
-  uint32_t pad;
+  uint32_t n_tiles;  // work-item slots: tiles x parts
+  uint32_t parts;    // shares of each tile's source window
 };
 
 // Search state of one column (hestimate.cpp:55-86 recursion, unrolled).
@@ -53,25 +53,43 @@ struct HestState {
 };
 
 // Sequential float sums in the reference's order give the reference's h0
-// bit for bit (Boost lazy variance over float, hestimate.cpp:19-30).
+// bit for bit (Boost lazy variance over float, hestimate.cpp:19-30). One warp
+// per column: the lanes load 32 consecutive values at a time (coalesced, the
+// next group in flight) and every lane adds them in element order from
+// shuffles, so each lane holds the same sequential sums. With with_h0 = 0
+// (a plain convolution) only n is recorded.
 __global__ void k_thumb(const ConvCol* __restrict__ cols, const float* __restrict__ raw,
                         const uint64_t* __restrict__ raw_off, const double* __restrict__ pw,
-                        HestState* __restrict__ st, uint32_t n_cols) {
-  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= n_cols) return;
-  const float* x = raw + raw_off[c];
+                        HestState* __restrict__ st, uint32_t n_cols, int with_h0) {
+  const uint32_t c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (c >= n_cols) return;  // warp-uniform
   const uint32_t n = cols[c].n;
-  float s = 0.f, s2 = 0.f;
-  for (uint32_t i = 0; i < n; ++i) {
-    const float v = x[i];
-    s = __fadd_rn(s, v);
-    s2 = __fadd_rn(s2, __fmul_rn(v, v));
+  if (!with_h0) {
+    if (lane == 0) st[c].n = n;
+    return;
   }
-  const float m2 = __fdiv_rn(s2, (float)n);
-  const float m = __fdiv_rn(s, (float)n);
-  const float var = __fsub_rn(m2, __fmul_rn(m, m));
-  st[c].h0 = (float)(pw[c] * sqrt((double)var));
-  st[c].n = n;
+  const float* x = raw + raw_off[c];
+  float s = 0.f, s2 = 0.f;
+  float nxt = lane < n ? x[lane] : 0.f;
+  for (uint32_t i0 = 0; i0 < n; i0 += 32) {
+    const float cur = nxt;
+    const uint32_t j = i0 + 32 + lane;
+    nxt = j < n ? x[j] : 0.f;
+    const uint32_t m = min(32u, n - i0);
+    for (uint32_t k = 0; k < m; ++k) {
+      const float v = __shfl_sync(0xffffffffu, cur, k);
+      s = __fadd_rn(s, v);
+      s2 = __fadd_rn(s2, __fmul_rn(v, v));
+    }
+  }
+  if (lane == 0) {
+    const float m2 = __fdiv_rn(s2, (float)n);
+    const float m = __fdiv_rn(s, (float)n);
+    const float var = __fsub_rn(m2, __fmul_rn(m, m));
+    st[c].h0 = (float)(pw[c] * sqrt((double)var));
+    st[c].n = n;
+  }
 }
 
 // raw_off: offset of each column in the raw coordinates; perm_off: offset of
@@ -164,8 +182,10 @@ __global__ void k_conv_plan(const ConvCol* __restrict__ cols, uint32_t n_cols,
   td.t_begin = 0;
   td.part = 0;
   td.pad = 0;
-  const uint32_t t = g - C.tile_base;
-  if (t < C.n_tiles) {
+  const uint32_t t = (g - C.tile_base) / C.parts;
+  const uint32_t part = (g - C.tile_base) % C.parts;
+  td.part = part;
+  if (t * tt < C.n) {
     const uint32_t tb = t * tt;
     const uint32_t tc = min(tt, C.n - tb);
     // widest support any level of the search can ask for: 2 * (2 h0)
@@ -187,6 +207,12 @@ __global__ void k_conv_plan(const ConvCol* __restrict__ cols, uint32_t n_cols,
     // symmetric: sources before the tile belong to earlier tiles, which
     // count each such pair twice (k_conv weights)
     a = max(a, tb);
+    if (C.parts > 1) {  // this slot's share of the window
+      const uint32_t w0 = e - a;
+      const uint32_t a1 = a + (uint32_t)((uint64_t)w0 * part / C.parts);
+      e = a + (uint32_t)((uint64_t)w0 * (part + 1) / C.parts);
+      a = a1;
+    }
     td.t_begin = tb;
     td.t_count = tc;
     td.n_runs = 1;
@@ -538,11 +564,21 @@ int hestimate_engine(Ctx& c, const float* raw, const std::vector<uint64_t>& raw_
   uint32_t slots = 0;
   std::vector<uint32_t> base(nc);
   std::vector<double> pw(nc);
+  // Few tiles for the persistent grid (a single column, say): split every
+  // tile's source window into up to 8 shares (work items); each share's
+  // partial sum has its own slot, so the per-column reduction is unchanged.
+  uint64_t tiles_all = 0;
+  for (uint32_t i = 0; i < nc; ++i) tiles_all += (lens[i] + tt_used - 1) / tt_used;
+  const uint64_t want = 16ull * (uint64_t)c.n_sms;
+  const uint32_t parts =
+      tiles_all > 0 && tiles_all < want
+          ? (uint32_t)std::min<uint64_t>(8, (want + tiles_all - 1) / tiles_all) : 1u;
   for (uint32_t i = 0; i < nc; ++i) {
     hc[i].n = lens[i];
     hc[i].xs = static_cast<float*>(c.arena.alloc(4 * ((size_t)lens[i] + 8)));
     if (!hc[i].xs) return c.fail(ENT_ERR_CUDA, "out of device memory");
-    hc[i].n_tiles = (lens[i] + tt_used - 1) / tt_used;
+    hc[i].parts = parts;
+    hc[i].n_tiles = (lens[i] + tt_used - 1) / tt_used * parts;
     hc[i].tile_base = slots;
     base[i] = slots;
     slots += hc[i].n_tiles;
@@ -574,7 +610,7 @@ int hestimate_engine(Ctx& c, const float* raw, const std::vector<uint64_t>& raw_
 
   const unsigned gx = std::min<uint32_t>((std::max(sv.max_n, 1u) + 255) / 256 + 1, 1024);
   k_gather_sorted<<<dim3(gx, nc), 256, 0, s>>>(dcols, raw, doff, sv.perm, dpoff);
-  k_thumb<<<(nc + 63) / 64, 64, 0, s>>>(dcols, raw, doff, dpw, dst, nc);
+  k_thumb<<<(nc + 3) / 4, 128, 0, s>>>(dcols, raw, doff, dpw, dst, nc, mode == 0 ? 0 : 1);
   k_hest_init<<<(nc + 63) / 64, 64, 0, s>>>(
       dst, nc, (mode == 0 || (mode == 2 && !d_log_ratio)) ? dhin : nullptr,
       mode == 2 ? skip : 0, mode == 0 ? 1 : 0, mode == 2 ? d_log_ratio : nullptr);
