@@ -191,21 +191,44 @@ __global__ void __launch_bounds__(NW * 32, MINB)
               // source-side sum over the warp's R targets in 4 interleaved
               // partials (short rounding and dependency chains)
               float src[4] = {0.f, 0.f, 0.f, 0.f};
+              if constexpr (D == 3) {
+                // two targets per step, their chains interleaved
 #pragma unroll
-              for (int r = 0; r < R; ++r) {
-                float dx, dy;
-                upk2(sub2(T01[r], S), dx, dy);
-                const float wx = __saturatef(__fmaf_rn(-dx, dx, g2a));
-                const float wy = __saturatef(__fmaf_rn(-dy, dy, g2b));
-                if constexpr (D == 2) {
-                  acc[r] = __fmaf_rn(wx, wy, acc[r]);
-                  src[r & 3] = __fmaf_rn(wx, wy, src[r & 3]);
-                } else {
-                  const float dz = T2[r] - s.z;
-                  const float wz = __saturatef(__fmaf_rn(-dz, dz, g2c));
-                  const float wxy = wx * wy;
-                  acc[r] = __fmaf_rn(wxy, wz, acc[r]);
-                  src[r & 3] = __fmaf_rn(wxy, wz, src[r & 3]);
+                for (int r = 0; r < R / 2; ++r) {
+                  const int q = r + R / 2;
+                  float dxa, dya, dxb, dyb;
+                  upk2(sub2(T01[r], S), dxa, dya);
+                  upk2(sub2(T01[q], S), dxb, dyb);
+                  const float dza = T2[r] - s.z, dzb = T2[q] - s.z;
+                  const float wxa = __saturatef(__fmaf_rn(-dxa, dxa, g2a));
+                  const float wxb = __saturatef(__fmaf_rn(-dxb, dxb, g2a));
+                  const float wya = __saturatef(__fmaf_rn(-dya, dya, g2b));
+                  const float wyb = __saturatef(__fmaf_rn(-dyb, dyb, g2b));
+                  const float wza = __saturatef(__fmaf_rn(-dza, dza, g2c));
+                  const float wzb = __saturatef(__fmaf_rn(-dzb, dzb, g2c));
+                  const float pa = wxa * wya, pb = wxb * wyb;
+                  acc[r] = __fmaf_rn(pa, wza, acc[r]);
+                  acc[q] = __fmaf_rn(pb, wzb, acc[q]);
+                  src[r & 3] = __fmaf_rn(pa, wza, src[r & 3]);
+                  src[q & 3] = __fmaf_rn(pb, wzb, src[q & 3]);
+                }
+              }
+              if constexpr (D == 2) {
+                // two targets per step, their chains interleaved
+#pragma unroll
+                for (int r = 0; r < R / 2; ++r) {
+                  const int q = r + R / 2;
+                  float dxa, dya, dxb, dyb;
+                  upk2(sub2(T01[r], S), dxa, dya);
+                  upk2(sub2(T01[q], S), dxb, dyb);
+                  const float wxa = __saturatef(__fmaf_rn(-dxa, dxa, g2a));
+                  const float wxb = __saturatef(__fmaf_rn(-dxb, dxb, g2a));
+                  const float wya = __saturatef(__fmaf_rn(-dya, dya, g2b));
+                  const float wyb = __saturatef(__fmaf_rn(-dyb, dyb, g2b));
+                  acc[r] = __fmaf_rn(wxa, wya, acc[r]);
+                  acc[q] = __fmaf_rn(wxb, wyb, acc[q]);
+                  src[r & 3] = __fmaf_rn(wxa, wya, src[r & 3]);
+                  src[q & 3] = __fmaf_rn(wxb, wyb, src[q & 3]);
                 }
               }
               myrow[s0 + k] = (src[0] + src[1]) + (src[2] + src[3]);
