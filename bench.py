@@ -330,6 +330,8 @@ def other_configs(ctx):
         ctx.combined_densities(xq, None, list(range(xq.shape[0])), hq)
     seq = time.perf_counter() - t0
     out["uneven_512"] = {"batched_ms": st.total_ms, "sequential_plain_s": seq, "autotuned": utuned,
+                         "pair_kernel_ms_by_dim": list(st.pair_kernel_ms_by_dim),
+                         "candidate_pairs_by_dim": list(st.candidate_pairs_by_dim),
                          "speedup": seq / (st.total_ms / 1e3), "support_pairs": supu,
                          "pairs_per_s": supu / (st.total_ms / 1e3),
                          "points": int(sum(xq.shape[1] for xq, _ in ub))}
