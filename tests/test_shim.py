@@ -63,3 +63,45 @@ def test_mi_driver_matches_reference(golden):
         ref = golden["est_mi"]
         # the reference prints 6 significant digits
         assert np.allclose(mi, ref, rtol=2e-5, atol=1e-5)
+
+
+def _build_abi_driver(td) -> Path:
+    _build_lib()
+    exe = Path(td, "abi_driver")
+    subprocess.run(["g++", "-std=c++14", "-O2", "-Wall", "-Werror",
+                    str(ROOT / "tests" / "cpp" / "abi_driver.cpp"), "-I", str(ROOT / "include"),
+                    "-L", str(LIB), "-lentropical_gb300", f"-Wl,-rpath,{LIB}", "-o", str(exe)],
+                   check=True)
+    return exe
+
+
+def test_abi_driver_compiles():
+    """The C header is usable from C++ as a plain C ABI (no CUDA headers)."""
+    with tempfile.TemporaryDirectory() as td:
+        assert _build_abi_driver(td).exists()
+
+
+@pytest.mark.gpu
+def test_abi_driver_matches_python_path(golden):
+    """C++ through the C ABI: file reader, autotuner, the reference's MI formula
+    and the resubstitution MI batch give the Python mirror's numbers and the
+    reference's MI output."""
+    from entropical_gb300 import Context
+    from entropical_gb300.densities import REF_MI
+    x = golden["est_x"].astype(np.float32)
+    with tempfile.TemporaryDirectory() as td:
+        exe = _build_abi_driver(td)
+        txt = Path(td, "coords.txt")
+        np.savetxt(txt, x.T, fmt="%.9g")
+        out = Path(td, "out.bin")
+        subprocess.run([str(exe), str(txt), "0.4", str(out)], check=True)
+        v = np.fromfile(out, np.float64)
+        m = int(v[0])
+        mi_ref = v[1:1 + m * m].reshape(m, m)
+        mi = v[1 + m * m:1 + 2 * m * m].reshape(m, m)
+        hx = v[1 + 2 * m * m:]
+    h = np.full(m, 0.4, np.float32)
+    with Context(0) as ctx:
+        assert np.allclose(mi_ref, ctx.reference_estimator(x, h, REF_MI), rtol=1e-9, atol=1e-12)
+        mi_p, hx_p = ctx.mi_all_pairs(x, h)
+        assert np.allclose(mi, mi_p, atol=1e-7) and np.allclose(hx, hx_p, atol=1e-7)
