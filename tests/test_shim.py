@@ -102,6 +102,8 @@ def test_abi_driver_matches_python_path(golden):
         hx = v[1 + 2 * m * m:]
     h = np.full(m, 0.4, np.float32)
     with Context(0) as ctx:
-        assert np.allclose(mi_ref, ctx.reference_estimator(x, h, REF_MI), rtol=1e-9, atol=1e-12)
+        # the formula's float log of a density ratio moves by an ulp when the
+        # FP32 partial sums differ (the C++ context is autotuned): 1e-6 relative
+        assert np.allclose(mi_ref, ctx.reference_estimator(x, h, REF_MI), rtol=1e-6, atol=1e-9)
         mi_p, hx_p = ctx.mi_all_pairs(x, h)
         assert np.allclose(mi, mi_p, atol=1e-7) and np.allclose(hx, hx_p, atol=1e-7)
