@@ -85,3 +85,14 @@ def test_te_support_counts(ctx):
     # 3-D instance (y+, y, x) for i=1, j=2
     c = ctx.support_counts(x, None, [1, 1, 2], [h[1], h[1], h[2]], [2, 0, 0])
     assert cnt[0, 1, 2] == c.sum()
+
+
+def test_mi_split_form_matches_batch(ctx):
+    """The densities of one all-pairs MI dealt out as shares (here one rank)
+    through entropy batches give the MI batch's numbers."""
+    from entropical_gb300.replicas import mi_all_pairs_sharded
+    x = workloads.mi_coords(6000, 5, seed=21)
+    h = workloads.scott_bandwidth(x, 2)
+    mi_s, hx_s = mi_all_pairs_sharded(ctx.entropy_batch, x, h)
+    mi, hx = ctx.mi_all_pairs(x, h)
+    assert np.max(np.abs(mi_s - mi)) < 1e-7 and np.max(np.abs(hx_s - hx)) < 1e-7
