@@ -128,8 +128,6 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
   s = t;
 }
 
-// Orderable 32-bit key of a float: unsigned compare == float compare
-// (-0.0 sorts just before +0.0; NaN never reaches here).
 // float -> double by re-biasing the IEEE-754 fields on the integer pipes
 // (exact for normal floats; zero and subnormals give 0). The FP64 pipe of
 // this GPU runs at a small fraction of the FP32 rate, so conversions on the
@@ -175,6 +173,8 @@ __device__ __forceinline__ double log_fp64(double x, const double2* __restrict__
   return fma(de, l2.x, t.y) + fma(de, l2.y, p);
 }
 
+// Orderable 32-bit key of a float: unsigned compare == float compare
+// (-0.0 sorts just before +0.0; NaN never reaches here).
 __device__ __forceinline__ uint32_t float_key(float f) {
   uint32_t u = __float_as_uint(f);
   return (u & 0x80000000u) ? ~u : (u | 0x80000000u);

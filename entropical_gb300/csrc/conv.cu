@@ -9,13 +9,14 @@
 //   bracket [0.1 h0, 2 h0], prec 0.01 h0: at each level evaluate amise at the
 //   two quarter points and keep the half on the side of the smaller value.
 //
-// Columns are value-sorted once (radix sort of the engine); each target tile
-// of the sorted column sees one contiguous run of sources within 2 h_max,
-// staged into shared memory with TMA bulk copies exactly as in the density
-// kernel. One pass evaluates BOTH pivots of a level (packed f32x2 over the
-// two bandwidths). The per-column search state lives on the device; each
-// level is conv -> per-column reduce -> decide, all columns at once, and the
-// level sequence is captured into one CUDA graph.
+// Columns are value-sorted once (radix sort of the engine). In a sorted
+// column the support of target i is one contiguous index range, so C(h) is
+// evaluated from FP64 prefix sums of the centred values: per target one
+// binary search for the end of its range and a few FP64 operations
+// (k_conv_range), O(n log n) per bandwidth instead of O(n * support). The
+// per-column search state lives on the device; each level is conv (both
+// pivots) -> per-column reduce -> decide, all columns at once, and the level
+// sequence is captured into one CUDA graph.
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
@@ -24,18 +25,19 @@
 #include "../../include/entropical_gb300.h"
 #include "api_internal.h"
 #include "engine.h"
-#include "staging.cuh"
+#include "staging.cuh"  // FULL_MASK
 
 using namespace ent;
 
 namespace {
 
 struct ConvCol {
-  const float* xs;  // value-sorted column (n + 8 floats)
+  const float* xs;      // value-sorted column (n + 8 floats)
+  double* P;            // P[k] = sum_{j<k} (xs[j] - xs[n/2]), k = 0..n
   uint32_t n;
-  uint32_t tile_base;
-  uint32_t n_tiles;  // work-item slots: tiles x parts
-  uint32_t parts;    // shares of each tile's source window
+  uint32_t tile_base;   // first target block (slot) of the column
+  uint32_t n_tiles;     // target blocks: ceil(n / CONV_TB)
+  uint32_t chunk_base;  // first prefix chunk of the column
 };
 
 // Search state of one column (hestimate.cpp:55-86 recursion, unrolled).
@@ -163,242 +165,192 @@ __global__ void k_hest_init(HestState* __restrict__ st, uint32_t n_cols,
   st[c] = s;
 }
 
-__global__ void k_conv_plan(const ConvCol* __restrict__ cols, uint32_t n_cols,
-                            const uint32_t* __restrict__ col_tile_base,
-                            const HestState* __restrict__ st, int fixed_h,
-                            TileDesc* __restrict__ tiles, uint32_t n_slots, uint32_t tt) {
-  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= n_slots) return;
+// ---------------------------------------------------------------- prefix
+// P[k] = sum_{j<k} (xs[j] - mu) in FP64 for every column, mu = xs[n/2]:
+// centring keeps the partial sums near the spread of the data, so the range
+// sums below lose few bits. Three passes: chunk totals, one warp scanning
+// each column's chunk totals, chunk-local scans from the chunk offsets. Every
+// sum runs in a fixed order, so P is deterministic.
+constexpr uint32_t CONV_TB = 256;                // targets per block of k_conv_range
+constexpr uint32_t PF_E = 8;                     // prefix values per thread
+constexpr uint32_t PF_CHUNK = CONV_TB * PF_E;    // prefix values per block
+
+__device__ __forceinline__ double col_centre(const ConvCol& C) {
+  return (double)C.xs[C.n / 2];
+}
+
+__global__ void __launch_bounds__(CONV_TB)
+    k_prefix_totals(const ConvCol* __restrict__ cols, double* __restrict__ chunk_tot) {
+  __shared__ double sw[CONV_TB / 32];
+  const ConvCol& C = cols[blockIdx.y];
+  const uint64_t b0 = (uint64_t)blockIdx.x * PF_CHUNK;
+  if (b0 >= C.n) return;  // block-uniform
+  const double mu = col_centre(C);
+  const uint64_t k0 = b0 + (uint64_t)threadIdx.x * PF_E;
+  double a = 0.0;
+#pragma unroll
+  for (uint32_t e = 0; e < PF_E; ++e)
+    if (k0 + e < C.n) a += (double)C.xs[k0 + e] - mu;
+  for (int o = 16; o; o >>= 1) a += __shfl_xor_sync(FULL_MASK, a, o);
+  if ((threadIdx.x & 31) == 0) sw[threadIdx.x >> 5] = a;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (uint32_t w = 0; w < CONV_TB / 32; ++w) t += sw[w];
+    chunk_tot[C.chunk_base + blockIdx.x] = t;
+  }
+}
+
+// One warp per column: exclusive scan of its chunk totals, in place.
+__global__ void k_prefix_chunks(const ConvCol* __restrict__ cols, uint32_t n_cols,
+                                double* __restrict__ chunk_tot) {
+  const uint32_t c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (c >= n_cols) return;  // warp-uniform
+  const uint32_t nch = (cols[c].n + PF_CHUNK - 1) / PF_CHUNK;
+  double* t = chunk_tot + cols[c].chunk_base;
+  double run = 0.0;
+  for (uint32_t b = 0; b < nch; b += 32) {
+    const double v = b + lane < nch ? t[b + lane] : 0.0;
+    double inc = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const double u = __shfl_up_sync(FULL_MASK, inc, o);
+      if (lane >= o) inc += u;
+    }
+    double exc = __shfl_up_sync(FULL_MASK, inc, 1);
+    if (lane == 0) exc = 0.0;
+    if (b + lane < nch) t[b + lane] = run + exc;
+    run += __shfl_sync(FULL_MASK, inc, 31);
+  }
+}
+
+__global__ void __launch_bounds__(CONV_TB)
+    k_prefix_write(const ConvCol* __restrict__ cols, const double* __restrict__ chunk_off) {
+  __shared__ double sw[CONV_TB / 32];
+  const ConvCol& C = cols[blockIdx.y];
+  const uint64_t b0 = (uint64_t)blockIdx.x * PF_CHUNK;
+  if (b0 >= C.n) return;  // block-uniform
+  const double mu = col_centre(C);
+  const uint64_t k0 = b0 + (uint64_t)threadIdx.x * PF_E;
+  double v[PF_E];
+  double tot = 0.0;
+#pragma unroll
+  for (uint32_t e = 0; e < PF_E; ++e) {
+    if (k0 + e < C.n) tot += (double)C.xs[k0 + e] - mu;
+    v[e] = tot;  // inclusive within the thread
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double inc = tot;
+  for (int o = 1; o < 32; o <<= 1) {
+    const double u = __shfl_up_sync(FULL_MASK, inc, o);
+    if (lane >= o) inc += u;
+  }
+  if (lane == 31) sw[warp] = inc;
+  __syncthreads();
+  double base = chunk_off[C.chunk_base + blockIdx.x];
+  for (int w = 0; w < warp; ++w) base += sw[w];
+  double exc = __shfl_up_sync(FULL_MASK, inc, 1);
+  if (lane == 0) exc = 0.0;
+  base += exc;
+  double* P = C.P;
+  if (b0 == 0 && threadIdx.x == 0) P[0] = 0.0;
+#pragma unroll
+  for (uint32_t e = 0; e < PF_E; ++e)
+    if (k0 + e < C.n) P[k0 + e + 1] = base + v[e];
+}
+
+// --------------------------------------------------------- convolution
+// C(h) n^2 = sum_i sum_j K_ij with K_ij = 4.5 - 2.25 |x_i - x_j| / h on the
+// support |x_i - x_j| <= 2h. The support is symmetric and, in a sorted
+// column, contiguous: for target i the partners j > i are i+1 .. e_i - 1,
+// e_i the first index with fl(x_j - x_i) > 2h (a monotone predicate, found
+// by binary search). With c_i = e_i - 1 - i partners and
+// S_i = sum_{j=i+1}^{e_i-1} (x_j - x_i) = (P[e_i] - P[i+1]) - c_i (x_i - mu),
+//   sum_j K_ij over j > i = 4.5 c_i - 2.25 S_i / h,
+// and the double sum is 4.5 n + 2 sum_i (4.5 c_i - 2.25 S_i / h): exact
+// arithmetic on the same support as the reference's per-pair loop
+// (densities_omp.cpp:247-272), O(log n) per target instead of O(support).
+// One thread per target, CONV_TB targets per block; NP bandwidths per pass
+// (1: plain epa_convolution, 2: both pivots of a search level). Each block
+// writes its partial double sums to its slot; k_conv_reduce adds the slots
+// of a column in a fixed order.
+template <int NP>
+__global__ void __launch_bounds__(CONV_TB)
+    k_conv_range(const ConvCol* __restrict__ cols, uint32_t n_cols,
+                 const uint32_t* __restrict__ col_tile_base, const HestState* __restrict__ st,
+                 double* __restrict__ tile_sum) {
+  __shared__ double sA[NP][CONV_TB / 32];
+  __shared__ unsigned long long sC[NP][CONV_TB / 32];
+  const uint32_t g = blockIdx.x;
   uint32_t lo = 0, hi = n_cols;
   while (hi - lo > 1) {
     const uint32_t m = (lo + hi) / 2;
     if (col_tile_base[m] <= g) lo = m; else hi = m;
   }
   const ConvCol& C = cols[lo];
-  TileDesc td;
-  td.inst = lo;
-  td.n_runs = 0;
-  td.t_count = 0;
-  td.t_begin = 0;
-  td.part = 0;
-  td.pad = 0;
-  const uint32_t t = (g - C.tile_base) / C.parts;
-  const uint32_t part = (g - C.tile_base) % C.parts;
-  td.part = part;
-  if (t * tt < C.n) {
-    const uint32_t tb = t * tt;
-    const uint32_t tc = min(tt, C.n - tb);
-    // widest support any level of the search can ask for: 2 * (2 h0)
-    const float hmax = fixed_h ? st[lo].piv[0] : st[lo].ghi;
-    const float w = 2.f * hmax * (1.f + 1e-5f) + 1e-30f;
-    const float xf = C.xs[tb], xl = C.xs[tb + tc - 1];
-    const float eps = 1e-6f * (fabsf(xf) + fabsf(xl));
-    const float vlo = xf - w - eps, vhi = xl + w + eps;
-    uint32_t a = 0, b = C.n;
-    while (a < b) {
-      const uint32_t m = a + (b - a) / 2;
-      if (C.xs[m] < vlo) a = m + 1; else b = m;
-    }
-    uint32_t e = a, f = C.n;
-    while (e < f) {
-      const uint32_t m = e + (f - e) / 2;
-      if (C.xs[m] <= vhi) e = m + 1; else f = m;
-    }
-    // symmetric: sources before the tile belong to earlier tiles, which
-    // count each such pair twice (k_conv weights)
-    a = max(a, tb);
-    if (C.parts > 1) {  // this slot's share of the window
-      const uint32_t w0 = e - a;
-      const uint32_t a1 = a + (uint32_t)((uint64_t)w0 * part / C.parts);
-      e = a + (uint32_t)((uint64_t)w0 * (part + 1) / C.parts);
-      a = a1;
-    }
-    td.t_begin = tb;
-    td.t_count = tc;
-    td.n_runs = 1;
-    td.lo[0] = a;
-    td.len[0] = e - a;
+  if (st[lo].done) {  // block-uniform
+    if (threadIdx.x == 0) tile_sum[2 * (size_t)g] = tile_sum[2 * (size_t)g + 1] = 0.0;
+    return;
   }
-  tiles[g] = td;
-}
-
-// One pass over (target, source) pairs within the window evaluates the
-// convolution kernel at NP bandwidths (NP = 1: plain epa_convolution,
-// NP = 2: both pivots of a search level). The double sum is symmetric in
-// (i, j), so a tile of targets [tb, tb + tc) sees only sources from tb on:
-// sources inside the tile count once (both orders are target-side pairs),
-// sources after it count twice (weight 2, exact), sources before it are
-// counted by their own tile.
-template <int NP, int R>
-__global__ void __launch_bounds__(128)
-    k_conv(const TileDesc* __restrict__ tiles, uint32_t n_slots,
-           const ConvCol* __restrict__ cols, const HestState* __restrict__ st,
-           uint32_t* work_counter, uint32_t* err, double* __restrict__ tile_sum) {
-  typedef Cfg<1, R> CC;
-  extern __shared__ __align__(128) unsigned char dsm[];
-  float* bufs = reinterpret_cast<float*>(dsm);
-  __shared__ __align__(8) uint64_t full[2];
-  __shared__ Piece ptab[2][CC::MAXP];
-  __shared__ uint32_t npc[2];
-  __shared__ uint32_t run_lo[MAX_RUNS], run_pre[MAX_RUNS + 1];
-  __shared__ uint32_t s_g, s_nr, s_tb, s_tc, s_col, s_skip;
-  __shared__ double s_part[CC::NW][2];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (tid == 0) {
-    mbar_init(&full[0], 1);
-    mbar_init(&full[1], 1);
-    fence_mbar_init();
+  const uint32_t n = C.n;
+  const uint32_t blk = g - C.tile_base;
+  const uint32_t i = blk * CONV_TB + threadIdx.x;
+  const float* __restrict__ xs = C.xs;
+  const double* __restrict__ P = C.P;
+  float w[NP];
+#pragma unroll
+  for (int k = 0; k < NP; ++k) w[k] = 2.f * st[lo].piv[k];
+  double A[NP];
+  unsigned long long cnt[NP];
+#pragma unroll
+  for (int k = 0; k < NP; ++k) {
+    A[k] = 0.0;
+    cnt[k] = 0ull;
   }
-  __syncthreads();
-  uint32_t q = 0;
-  for (;;) {
-    if (tid == 0) {
-      const uint32_t g = atomicAdd(work_counter, 1u);
-      s_g = g;
-      if (g < n_slots) {
-        const TileDesc* T = tiles + g;
-        s_tb = T->t_begin;
-        s_tc = T->t_count;
-        s_col = T->inst;
-        s_nr = T->n_runs;
-        s_skip = (T->t_count == 0 || st[T->inst].done) ? 1u : 0u;
-        run_pre[0] = 0;
-        for (uint32_t r = 0; r < T->n_runs; ++r) {
-          run_lo[r] = T->lo[r];
-          run_pre[r + 1] = run_pre[r] + T->len[r];
-        }
-      }
-    }
-    __syncthreads();
-    const uint32_t g = s_g;
-    if (g >= n_slots) break;
-    if (s_skip) {
-      if (tid == 0) {
-        tile_sum[2 * (size_t)g] = 0.0;
-        tile_sum[2 * (size_t)g + 1] = 0.0;
-      }
-      __syncthreads();
-      continue;
-    }
-    const uint32_t tc = s_tc, tb = s_tb, nr = s_nr, nsrc = run_pre[nr];
-    const ConvCol& Cc = cols[s_col];
-    const float* __restrict__ xs = Cc.xs;
-    const uint32_t nch = (nsrc + CC::CH - 1) / CC::CH;
-    if (tid == 0 && nch > 0)
-      issue_chunk<CC>(0, q & 1u, nsrc, nr, run_lo, run_pre, xs, bufs, ptab, npc, full);
-    float coef[2];
-#pragma unroll
-    for (int k = 0; k < 2; ++k) coef[k] = -2.25f / st[s_col].piv[k];
-    float T[R];
-    float ks[NP][R], kc[NP][R];
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      const uint32_t li = warp * R + r;
-      T[r] = li < tc ? xs[tb + li] : 1e30f;
-#pragma unroll
-      for (int k = 0; k < NP; ++k) ks[k][r] = kc[k][r] = 0.f;
-    }
-    bool aborted = false;
-    uint32_t ab_q = 0;
-    bool ab_next = false;
-    for (uint32_t c = 0; c < nch; ++c) {
-      const uint32_t qq = q + c, b = qq & 1u;
-      if (tid == 0 && c + 1 < nch)
-        issue_chunk<CC>(c + 1, (qq + 1) & 1u, nsrc, nr, run_lo, run_pre, xs, bufs, ptab,
-                          npc, full);
-      const bool ok = mbar_wait(&full[b], (qq >> 1) & 1u);
-      if (ok) {
-        const float* B = bufs + (size_t)b * CC::CAP;
-        for (uint32_t pi = 0; pi < npc[b]; ++pi) {
-          const uint32_t s0 = ptab[b][pi].s0, n = ptab[b][pi].n;
-          // sorted position of the piece's first element
-          const uint32_t a0 = ptab[b][pi].g0 + (s0 - ptab[b][pi].o);
-          const uint32_t tend = tb + tc;
-          if constexpr (NP == 1) {
-            float acc[R];
-#pragma unroll
-            for (int r = 0; r < R; ++r) acc[r] = 0.f;
-#pragma unroll 2
-            for (uint32_t k = lane; k < n; k += 32) {
-              const float s = B[s0 + k];
-              const float wgt = a0 + k >= tend ? 2.f : 1.f;
-#pragma unroll
-              for (int r = 0; r < R; ++r) {
-                const float t = fabsf(T[r] - s);
-                acc[r] = fmaf(fmaxf(fmaf(t, coef[0], 4.5f), 0.f), wgt, acc[r]);
-              }
-            }
-#pragma unroll
-            for (int r = 0; r < R; ++r) kahan_add(ks[0][r], kc[0][r], acc[r]);
-          } else {
-            const f32x2 CO = pk2(coef[0], coef[1]);
-            const f32x2 F45 = pk2(4.5f, 4.5f);
-            f32x2 acc[R];
-#pragma unroll
-            for (int r = 0; r < R; ++r) acc[r] = pk2(0.f, 0.f);
-#pragma unroll 2
-            for (uint32_t k = lane; k < n; k += 32) {
-              const float s = B[s0 + k];
-              const float wgt = a0 + k >= tend ? 2.f : 1.f;
-              const f32x2 W = pk2(wgt, wgt);
-#pragma unroll
-              for (int r = 0; r < R; ++r) {
-                const float t = fabsf(T[r] - s);
-                const f32x2 w = fma2(pk2(t, t), CO, F45);
-                float w0, w1;
-                upk2(w, w0, w1);
-                acc[r] = fma2(pk2(fmaxf(w0, 0.f), fmaxf(w1, 0.f)), W, acc[r]);
-              }
-            }
-#pragma unroll
-            for (int r = 0; r < R; ++r) {
-              float a0, a1;
-              upk2(acc[r], a0, a1);
-              kahan_add(ks[0][r], kc[0][r], a0);
-              kahan_add(ks[1][r], kc[1][r], a1);
-            }
-          }
-        }
-      }
-      if (__syncthreads_or(!ok)) {
-        aborted = true;
-        ab_q = qq;
-        ab_next = c + 1 < nch;
-        break;
-      }
-    }
-    if (aborted) {
-      if (tid == 0) {
-        atomicOr(err, EF_TIMEOUT);
-        mbar_wait(&full[ab_q & 1u], (ab_q >> 1) & 1u);
-        if (ab_next) mbar_wait(&full[(ab_q + 1) & 1u], ((ab_q + 1) >> 1) & 1u);
-      }
-      __syncthreads();
-      return;
-    }
-    q += nch;
-    const int tgt = lane >> (5 - Log2<R>::v);
-    const bool writer = (lane & ((32 / R) - 1)) == 0;
-    const uint32_t li = warp * R + tgt;
+  if (i < n) {
+    const float xi = xs[i];
+    const double xc = (double)xi - col_centre(C);
+    const double p1 = P[i + 1];
 #pragma unroll
     for (int k = 0; k < NP; ++k) {
-      float v[R];
-#pragma unroll
-      for (int r = 0; r < R; ++r) v[r] = ks[k][r] - kc[k][r];
-      const float tot = warp_transpose_sum<R>(v, lane);
-      double part = (writer && li < tc) ? (double)tot : 0.0;
-      for (int o = 16; o; o >>= 1) part += __shfl_xor_sync(FULL_MASK, part, o);
-      if (lane == 0) s_part[warp][k] = part;
-    }
-    __syncthreads();
-    if (tid == 0) {
-#pragma unroll
-      for (int k = 0; k < 2; ++k) {
-        double t = 0.0;
-        if (k < NP)
-          for (int w = 0; w < CC::NW; ++w) t += s_part[w][k];
-        tile_sum[2 * (size_t)g + k] = t;
+      uint32_t a = i + 1, b = n;  // first j > i with fl(x_j - x_i) > 2h
+      while (a < b) {
+        const uint32_t m = a + ((b - a) >> 1);
+        if (__fsub_rn(xs[m], xi) > w[k]) b = m; else a = m + 1;
       }
+      const uint32_t c = a - 1 - i;
+      A[k] = fma(-(double)c, xc, P[a] - p1);
+      cnt[k] = c;
+    }
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NP; ++k) {
+    for (int o = 16; o; o >>= 1) {
+      A[k] += __shfl_xor_sync(FULL_MASK, A[k], o);
+      cnt[k] += __shfl_xor_sync(FULL_MASK, cnt[k], o);
+    }
+    if (lane == 0) {
+      sA[k][warp] = A[k];
+      sC[k][warp] = cnt[k];
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint32_t nb = min(CONV_TB, n - blk * CONV_TB);
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      double t = 0.0;
+      if (k < NP) {
+        double sa = 0.0;
+        unsigned long long sc = 0ull;
+        for (uint32_t q = 0; q < CONV_TB / 32; ++q) {
+          sa += sA[k][q];
+          sc += sC[k][q];
+        }
+        t = 4.5 * (double)nb + 9.0 * (double)sc - (4.5 / (double)st[lo].piv[k]) * sa;
+      }
+      tile_sum[2 * (size_t)g + k] = t;
     }
   }
 }
@@ -518,27 +470,6 @@ T* upload(Ctx& c, const std::vector<T>& v, cudaError_t* e) {
   return p;
 }
 
-template <int NP, int R>
-cudaError_t launch_conv_t(cudaStream_t s, const TileDesc* tiles, uint32_t n_slots,
-                          const ConvCol* cols, const HestState* st, uint32_t* wc,
-                          uint32_t* err, double* tile_sum, int n_sms) {
-  typedef Cfg<1, R> CC;
-  auto kern = k_conv<NP, R>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)CC::SMEM);
-  if (e != cudaSuccess) return e;
-  int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, CC::NT, CC::SMEM);
-  if (e != cudaSuccess) return e;
-  uint64_t grid = (uint64_t)std::max(per_sm, 1) * (uint64_t)n_sms;
-  grid = std::min<uint64_t>(grid, std::max<uint32_t>(n_slots, 1));
-  e = cudaMemsetAsync(wc, 0, sizeof(uint32_t), s);
-  if (e != cudaSuccess) return e;
-  kern<<<(unsigned)grid, CC::NT, CC::SMEM, s>>>(tiles, n_slots, cols, st, wc, err, tile_sum);
-  return cudaGetLastError();
-}
-
-constexpr int CONV_R1 = 16, CONV_R2 = 8;
 
 }  // namespace
 
@@ -559,29 +490,22 @@ int hestimate_engine(Ctx& c, const float* raw, const std::vector<uint64_t>& raw_
   SortedViews sv;
   int rs = sort_views(c, views, &sv);
   if (rs) return rs;
+  if (nc > 65535u) return c.fail(ENT_ERR_TOO_LARGE, "too many columns in one search");
   std::vector<ConvCol> hc(nc);
-  const uint32_t tt_used = mode == 0 ? Cfg<1, CONV_R1>::TT : Cfg<1, CONV_R2>::TT;
-  uint32_t slots = 0;
+  uint32_t slots = 0, chunks = 0;
   std::vector<uint32_t> base(nc);
   std::vector<double> pw(nc);
-  // Few tiles for the persistent grid (a single column, say): split every
-  // tile's source window into up to 8 shares (work items); each share's
-  // partial sum has its own slot, so the per-column reduction is unchanged.
-  uint64_t tiles_all = 0;
-  for (uint32_t i = 0; i < nc; ++i) tiles_all += (lens[i] + tt_used - 1) / tt_used;
-  const uint64_t want = 16ull * (uint64_t)c.n_sms;
-  const uint32_t parts =
-      tiles_all > 0 && tiles_all < want
-          ? (uint32_t)std::min<uint64_t>(8, (want + tiles_all - 1) / tiles_all) : 1u;
   for (uint32_t i = 0; i < nc; ++i) {
     hc[i].n = lens[i];
     hc[i].xs = static_cast<float*>(c.arena.alloc(4 * ((size_t)lens[i] + 8)));
-    if (!hc[i].xs) return c.fail(ENT_ERR_CUDA, "out of device memory");
-    hc[i].parts = parts;
-    hc[i].n_tiles = (lens[i] + tt_used - 1) / tt_used * parts;
+    hc[i].P = static_cast<double*>(c.arena.alloc(8 * ((size_t)lens[i] + 1)));
+    if (!hc[i].xs || !hc[i].P) return c.fail(ENT_ERR_CUDA, "out of device memory");
+    hc[i].n_tiles = (lens[i] + CONV_TB - 1) / CONV_TB;
     hc[i].tile_base = slots;
+    hc[i].chunk_base = chunks;
     base[i] = slots;
     slots += hc[i].n_tiles;
+    chunks += (lens[i] + PF_CHUNK - 1) / PF_CHUNK;
     pw[i] = std::pow((double)lens[i], -1.0 / 7.0);  // std::pow(n_rows, -1/7)
   }
   ConvCol* dcols = upload(c, hc, &e);
@@ -599,50 +523,44 @@ int hestimate_engine(Ctx& c, const float* raw, const std::vector<uint64_t>& raw_
   float* dhin = upload(c, hin, &e);
   if (e != cudaSuccess) return c.cuda_fail(e, "upload bandwidths");
   HestState* dst = static_cast<HestState*>(c.arena.alloc(sizeof(HestState) * nc));
-  TileDesc* tiles = static_cast<TileDesc*>(c.arena.alloc(sizeof(TileDesc) * std::max(slots, 1u)));
   double* tsum = static_cast<double*>(c.arena.alloc(16 * (size_t)std::max(slots, 1u)));
   double* csum = static_cast<double*>(c.arena.alloc(16 * (size_t)nc));
-  uint32_t* wc = static_cast<uint32_t*>(c.arena.alloc(16));
+  double* ctot = static_cast<double*>(c.arena.alloc(8 * (size_t)std::max(chunks, 1u)));
   float* dconv = static_cast<float*>(c.arena.alloc(8 * (size_t)nc * 24));
-  if (!dst || !tiles || !tsum || !csum || !wc || !dconv)
+  if (!dst || !tsum || !csum || !ctot || !dconv)
     return c.fail(ENT_ERR_CUDA, "out of device memory");
   cudaMemsetAsync(dst, 0, sizeof(HestState) * nc, s);
 
   const unsigned gx = std::min<uint32_t>((std::max(sv.max_n, 1u) + 255) / 256 + 1, 1024);
+  const unsigned gc = (std::max(sv.max_n, 1u) + PF_CHUNK - 1) / PF_CHUNK;
   k_gather_sorted<<<dim3(gx, nc), 256, 0, s>>>(dcols, raw, doff, sv.perm, dpoff);
   k_thumb<<<(nc + 3) / 4, 128, 0, s>>>(dcols, raw, doff, dpw, dst, nc, mode == 0 ? 0 : 1);
   k_hest_init<<<(nc + 63) / 64, 64, 0, s>>>(
       dst, nc, (mode == 0 || (mode == 2 && !d_log_ratio)) ? dhin : nullptr,
       mode == 2 ? skip : 0, mode == 0 ? 1 : 0, mode == 2 ? d_log_ratio : nullptr);
-  k_conv_plan<<<(std::max(slots, 1u) + 127) / 128, 128, 0, s>>>(dcols, nc, dbase, dst,
-                                                                 mode == 0 ? 1 : 0, tiles, slots,
-                                                                 tt_used);
-  c.stats.kernel_launches += 4;
+  k_prefix_totals<<<dim3(gc, nc), CONV_TB, 0, s>>>(dcols, ctot);
+  k_prefix_chunks<<<(nc + 3) / 4, 128, 0, s>>>(dcols, nc, ctot);
+  k_prefix_write<<<dim3(gc, nc), CONV_TB, 0, s>>>(dcols, ctot);
+  c.stats.kernel_launches += 6;
   if ((e = cudaGetLastError()) != cudaSuccess) return c.cuda_fail(e, "hestimate setup");
 
   cudaEventRecord(c.ev_k0, s);
   if (mode == 0) {
-    e = launch_conv_t<1, CONV_R1>(s, tiles, slots, dcols, dst, wc, c.d_err, tsum, c.n_sms);
-    if (e != cudaSuccess) return c.cuda_fail(e, "convolution kernel");
+    k_conv_range<1><<<slots, CONV_TB, 0, s>>>(dcols, nc, dbase, dst, tsum);
     k_conv_reduce<<<nc, 256, 0, s>>>(dcols, tsum, csum);
     k_conv_single_out<<<(nc + 63) / 64, 64, 0, s>>>(dst, nc, csum, dconv);
     c.stats.kernel_launches += 3;
+    if ((e = cudaGetLastError()) != cudaSuccess) return c.cuda_fail(e, "convolution kernel");
   } else {
     // The level loop (at most 20 levels; 8 for every finite h0 > 0) runs as
     // one captured CUDA graph of conv -> reduce -> decide per level.
     const int max_levels = 9 - (mode == 2 ? std::min(skip, 8) : 0);
-    typedef Cfg<1, CONV_R2> CC;
-    auto kern = k_conv<2, CONV_R2>;
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CC::SMEM);
-    if (e != cudaSuccess) return c.cuda_fail(e, "conv attributes");
-    const unsigned grid = c.persistent_grid(slots, (const void*)kern, CC::NT, CC::SMEM);
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return c.cuda_fail(e, "begin capture");
     for (int L = 0; L < max_levels; ++L) {
-      cudaMemsetAsync(wc, 0, sizeof(uint32_t), s);
-      kern<<<grid, CC::NT, CC::SMEM, s>>>(tiles, slots, dcols, dst, wc, c.d_err, tsum);
+      k_conv_range<2><<<slots, CONV_TB, 0, s>>>(dcols, nc, dbase, dst, tsum);
       k_conv_reduce<<<nc, 256, 0, s>>>(dcols, tsum, csum);
       k_hest_level<<<(nc + 63) / 64, 64, 0, s>>>(dst, nc, csum, dconv + 2 * (size_t)nc * L);
     }

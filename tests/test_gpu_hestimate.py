@@ -23,6 +23,19 @@ def test_convolution_fp64(ctx, n):
         assert abs(ctx.epa_convolution(x, h) - O.epa_conv_fp64(x, h)) / O.epa_conv_fp64(x, h) < 2e-6
 
 
+def test_convolution_offset_ties_and_size(ctx):
+    """Range sums from centred FP64 prefix sums: a column far from zero, a
+    column of heavy ties and a longer column, each against the FP64 oracle."""
+    base = workloads.gmm_1d(20000, seed=31)
+    cases = [(np.sort(base + np.float32(1000.0)), (0.02, 0.5)),
+             (np.sort(np.round(base, 2).astype(np.float32)), (0.004, 0.05, 0.6)),
+             (np.sort(workloads.gmm_1d(200000, seed=32)), (0.005, 0.08))]
+    for x, hs in cases:
+        for h in hs:
+            ref = O.epa_conv_fp64(x, h)
+            assert abs(ctx.epa_convolution(x, h) - ref) / ref < 2e-6
+
+
 def test_convolution_unsorted_input(ctx):
     x = workloads.gmm_1d(3000, seed=4)
     assert abs(ctx.epa_convolution(x, 0.1) - O.epa_conv_fp64(np.sort(x), 0.1)) < 1e-6
