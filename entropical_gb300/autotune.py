@@ -4,7 +4,8 @@ The persistent pair kernel has three knobs per density dimension d: targets
 per warp R (tile = 4 R targets), cells per bandwidth S along dimension 1 of
 2-D strips (dimensions 1 and 2 of 3-D strips), and the pair body (0: packed sub/fma + min; 1: saturating FMA;
 2: saturating at 5 CTAs/SM; 3: as 2 with larger chunks; 4: symmetric, each
-unordered pair once, at 5 CTAs/SM; 5: symmetric at 4 CTAs/SM).
+unordered pair once, 4 warps of 32 targets; 5: symmetric, 8 warps of 16;
+6, d = 1 only: range sums from exact prefix sums, no pair loop).
 ``tune`` times every supported combination on a sample of the caller's own
 batch (the first few instances, device time of the pair kernel of that
 dimension) and keeps the fastest; results are cached in a JSON file keyed by
@@ -21,7 +22,8 @@ from pathlib import Path
 from .densities import Context
 
 CANDIDATES = {
-    1: [(8, 2, 0), (16, 2, 0), (16, 2, 1), (16, 2, 2), (16, 2, 3), (16, 2, 4), (16, 2, 5)],
+    1: [(8, 2, 0), (16, 2, 0), (16, 2, 1), (16, 2, 2), (16, 2, 3), (16, 2, 4), (16, 2, 5),
+        (16, 2, 6)],
     2: [(8, 2, 0), (16, 1, 2), (16, 2, 0), (16, 2, 1), (16, 2, 2), (16, 2, 3),
         (16, 1, 4), (16, 2, 4), (16, 2, 5)],
     3: [(4, 1, 0), (8, 1, 0), (8, 1, 1), (8, 1, 2), (8, 2, 2), (8, 1, 3), (8, 1, 4), (8, 2, 4),

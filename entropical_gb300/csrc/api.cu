@@ -286,9 +286,9 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
   for (int d = 1; d <= 3; ++d) {
     int v = c.pair_variant[d - 1];
     if (!density_variant_supported(d, c.tile_r[d - 1], v)) v = 0;
-    if (pair_is_sym(v) && (mode & DM_COUNT)) v = 2;
+    if (pair_uses_acc(v) && (mode & DM_COUNT)) v = 2;
     var_d[d] = v;
-    sym_d[d] = pair_is_sym(v);
+    sym_d[d] = pair_uses_acc(v);
   }
   uint64_t sym_points = 0;
   for (int d = 1; d <= 3; ++d) {
@@ -360,7 +360,7 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
       if ((int)insts[i].d == d) tiles_d += hi[i].tile_cap;
     uint32_t parts = 1;
     const uint64_t want = 16ull * (uint64_t)c.n_sms;
-    if (sym_d[d] && tiles_d > 0 && tiles_d < want)
+    if (pair_is_sym(var_d[d]) && tiles_d > 0 && tiles_d < want)
       parts = (uint32_t)std::min<uint64_t>(8, (want + tiles_d - 1) / tiles_d);
     for (uint32_t i : order) {
       if ((int)insts[i].d != d) continue;
@@ -405,6 +405,41 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
         hi[i].acc = sym_acc + o;
         o += hi[i].n;
       }
+  }
+  // 1-D instances on the range-sum body: prefix sums and target blocks
+  std::vector<Range1D> r1;
+  std::vector<uint32_t> r1_blk;
+  uint32_t r1_chunks = 0, r1_blocks = 0, r1_max_n = 0;
+  if (var_d[1] == PAIR_RANGE) {
+    for (uint32_t i : order) {
+      if (hi[i].d != 1) continue;
+      Range1D r;
+      r.y = static_cast<const float*>(hi[i].pts);
+      r.acc = hi[i].acc;
+      r.P = c.arena.alloc(range1d_prefix_bytes(hi[i].n));
+      if (!r.P) return c.fail(ENT_ERR_CUDA, "out of device memory");
+      r.n = hi[i].n;
+      r.g2 = hi[i].g2[0];
+      r.chunk_base = r1_chunks;
+      r.blk_base = r1_blocks;
+      r1_chunks += range1d_chunks(r.n);
+      r1_blocks += range1d_blocks(r.n);
+      r1_max_n = std::max(r1_max_n, r.n);
+      r1.push_back(r);
+      r1_blk.push_back(r.blk_base);
+    }
+    if (r1.size() > 65535u) return c.fail(ENT_ERR_TOO_LARGE, "too many 1-D instances in one batch");
+  }
+  Range1D* dr1 = nullptr;
+  uint32_t* dr1_blk = nullptr;
+  void* r1_tot = nullptr;
+  if (!r1.empty()) {
+    dr1 = arena_upload(c, r1, &e);
+    if (e != cudaSuccess) return c.cuda_fail(e, "upload 1-D ranges");
+    dr1_blk = arena_upload(c, r1_blk, &e);
+    if (e != cudaSuccess) return c.cuda_fail(e, "upload 1-D blocks");
+    r1_tot = c.arena.alloc(32 * (size_t)r1_chunks);
+    if (!r1_tot) return c.fail(ENT_ERR_CUDA, "out of device memory");
   }
   uint32_t *sk = nullptr, *svals = nullptr, *sk2 = nullptr, *sv2 = nullptr;
   int strip_bits = bits_for(max_strips);
@@ -502,9 +537,14 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
       if (group_slots[d] == 0) continue;
       int launched = 0;
       rec(c.ev_d[d - 1][0]);
-      r = launch_density(st, d, c.tile_r[d - 1], var_d[d], tiles + group_base[d],
-                         group_slots[d], di_sorted, wc + d, c.d_err, tile_ls + group_base[d],
-                         mode, c.n_sms, &launched);
+      if (d == 1 && var_d[1] == PAIR_RANGE) {
+        r = launch_range1d(st, dr1, (uint32_t)r1.size(), r1_max_n, dr1_blk, r1_blocks, r1_tot);
+        launches += 3;
+      } else {
+        r = launch_density(st, d, c.tile_r[d - 1], var_d[d], tiles + group_base[d],
+                           group_slots[d], di_sorted, wc + d, c.d_err, tile_ls + group_base[d],
+                           mode, c.n_sms, &launched);
+      }
       if (r != cudaSuccess) return r;
       rec(c.ev_d[d - 1][1]);
       c.ran_d[d - 1] = true;
@@ -706,8 +746,9 @@ int ent_set_tuning(ent_ctx* ctx, const ent_tuning* t) {
   if (t->cells_per_h3 > 2) return c->fail(ENT_ERR_ARG, "cells_per_h3 must be 1..2");
   if (t->pair_variant > PAIR_SYM + 2) return c->fail(ENT_ERR_ARG, "pair_variant must be 0..6");
   for (int d = 0; d < 3; ++d)
-    if (t->pair_variant_by_dim[d] > PAIR_SYM + 2)
-      return c->fail(ENT_ERR_ARG, "pair_variant must be 0..6");
+    if (t->pair_variant_by_dim[d] > (d == 0 ? PAIR_RANGE + 1 : PAIR_SYM + 2))
+      return c->fail(ENT_ERR_ARG, d == 0 ? "pair_variant_by_dim[0] must be 0..7"
+                                          : "pair_variant_by_dim[1..2] must be 0..6");
   if (t->pair_variant)
     for (int d = 0; d < 3; ++d) c->pair_variant[d] = (int)t->pair_variant - 1;
   for (int d = 0; d < 3; ++d)

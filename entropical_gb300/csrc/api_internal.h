@@ -52,7 +52,8 @@ struct Ctx {
   int tile_r[3] = {16, 16, 8};  // targets per warp of the pair kernel, by d
   // pair body per dimension: 0 min-based, 1 saturating FMA, 2 saturating at
   // 5 CTAs/SM, 3 as 2 with larger chunks (fastest measured: 2, 2, 1)
-  int pair_variant[3] = {4, 4, 4};  // PAIR_SYM (engine.h): symmetric bodies
+  // PAIR_RANGE for d = 1, PAIR_SYM for d = 2, 3 (engine.h)
+  int pair_variant[3] = {6, 4, 4};
   bool use_graphs = true;       // capture the batch kernel sequence in a CUDA graph
 
   // grid of a persistent kernel: resident CTAs per SM x SMs, capped by work

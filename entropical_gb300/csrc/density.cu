@@ -718,6 +718,7 @@ __global__ void __launch_bounds__(256)
 int density_variant_supported(int d, int r, int v) {
   if (v == 0) return density_r_supported(d, r);
   if (pair_is_sym(v)) return d >= 1 && d <= 3;  // own tile shape, sym_tile_r
+  if (v == PAIR_RANGE) return d == 1;            // range sums: tiles only finish
   return v >= 1 && v <= 3 && r == (d == 3 ? 8 : 16);
 }
 

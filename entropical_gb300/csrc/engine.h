@@ -110,7 +110,8 @@ cudaError_t launch_plan(cudaStream_t st, const InstDev* insts, uint32_t n_inst,
                         const uint32_t* inst_tile_base, TileDesc* tiles,
                         uint32_t n_slots, uint64_t* n_src_total);
 // v: pair body, 0 = min-based, 1 = saturating FMA (needs g^2 < 1), 2-3 as 1
-// with other occupancy / chunk sizes, 4-5 symmetric (PAIR_SYM; r ignored)
+// with other occupancy / chunk sizes, 4-5 symmetric (PAIR_SYM; r ignored),
+// 6 range sums (PAIR_RANGE, d = 1; not launched through here)
 cudaError_t launch_density(cudaStream_t st, int d, int r, int v, const TileDesc* tiles,
                            uint32_t n_slots, const InstDev* insts,
                            uint32_t* work_counter, uint32_t* err,
@@ -135,8 +136,31 @@ constexpr int PAIR_SYM = 4;
 __host__ __device__ constexpr bool pair_is_sym(int v) {
   return v == PAIR_SYM || v == PAIR_SYM + 1;
 }
+// Pair body PAIR_RANGE (d = 1 only, range1d.cu): the support of a target in
+// the value-sorted points is one index range, so its sum comes from exact
+// fixed-point prefix sums after two binary searches. It writes InstDev::acc
+// and is finished by launch_sym_finish like the symmetric bodies.
+constexpr int PAIR_RANGE = 6;
+__host__ __device__ constexpr bool pair_uses_acc(int v) {
+  return pair_is_sym(v) || v == PAIR_RANGE;
+}
 int sym_tile_r(int d, int v);
 int sym_tile_targets(int d, int v);
+struct Range1D {
+  const float* y;       // value-sorted scaled points (InstDev::pts)
+  double* acc;          // unscaled sums by sorted position (InstDev::acc)
+  void* P;              // (n + 1) x {sum Y, sum Y^2}, 128-bit each
+  uint32_t n;
+  float g2;
+  uint32_t chunk_base;  // first prefix chunk of the instance
+  uint32_t blk_base;    // first target block of the instance
+};
+uint32_t range1d_chunks(uint32_t n);
+uint32_t range1d_blocks(uint32_t n);
+size_t range1d_prefix_bytes(uint32_t n);
+// rs: 1-D instances in ascending blk_base; chunk_tot: 32 B per chunk
+cudaError_t launch_range1d(cudaStream_t st, const Range1D* rs, uint32_t n_inst, uint32_t max_n,
+                           const uint32_t* blk_base, uint32_t n_blocks, void* chunk_tot);
 cudaError_t launch_density_sym(cudaStream_t st, int d, int v, const TileDesc* tiles,
                                uint32_t n_slots, const InstDev* insts,
                                uint32_t* work_counter, uint32_t* err, int n_sms,

@@ -152,8 +152,9 @@ class Context:
         """Tile shapes and pair body (0 min-based, 1 saturating FMA, 2 the same at
         5 CTAs/SM, 3 as 2 with larger chunks, 4 symmetric with 4 warps of 32
         targets, 5 symmetric with 8 warps of 16) for every dimension, or a list
-        of three per-dimension bodies; cells per bandwidth of the strips for
-        d = 2 (1..4) and d = 3 (1..2); 0/None keeps."""
+        of three per-dimension bodies (the first may also be 6: 1-D range sums
+        from exact prefix sums, the default for d = 1); cells per bandwidth of
+        the strips for d = 2 (1..4) and d = 3 (1..2); 0/None keeps."""
         t = _native.Tuning()
         for i, v in enumerate(targets_per_warp):
             t.targets_per_warp[i] = int(v)

@@ -74,10 +74,16 @@ typedef struct {
                                    added to both points; support counts use
                                    3 instead; own tiles of 128/128/64
                                    targets), 6 = as 5 with tiles of
-                                   64/64/32 targets; default 5 for every
-                                   dimension (get reports dimension 2) */
+                                   64/64/32 targets; default 5 for
+                                   dimensions 2 and 3 (get reports
+                                   dimension 2) */
   uint32_t pair_variant_by_dim[3]; /* the same per dimension (0 = keep);
-                                      applied after pair_variant */
+                                      applied after pair_variant; for
+                                      dimension 1 also 7 = range sums (no
+                                      pair loop: each target's support is
+                                      one range of the value-sorted points,
+                                      summed from exact fixed-point prefix
+                                      sums), the default for d = 1 */
   uint32_t cells_per_h3;        /* d=3 strips: cells per bandwidth along
                                    dimensions 1 and 2, 1..2 (default 1) */
 } ent_tuning;
