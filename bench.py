@@ -134,6 +134,54 @@ def fp32_peak_tflops(n_sms: int) -> tuple[float, str]:
                   "(no measured FP32 figure in MEASURED_PEAKS.json)")
 
 
+# Algorithmic HBM bytes per 2-D point of the strip-moment kernels (one MI
+# step): the point (8 B) read by the strip-extent, moment-total, prefix-write
+# and target kernels (4 x 8), the 128 B moment prefix row written once and
+# read at least once (2 x 128), the strip key (4) and the FP64 sum (8).
+MOMENT_BYTES_PER_POINT = 4 * 8 + 2 * 128 + 4 + 8
+
+
+def profile_figure(name: str, key: str) -> float | None:
+    """A figure `key = value` from a committed ncu summary under profiles/."""
+    p = ROOT / "profiles" / name
+    if not p.exists():
+        return None
+    for ln in p.read_text().splitlines():
+        if ln.startswith(key):
+            try:
+                return float(ln.split("=", 1)[1].split()[0])
+            except Exception:
+                return None
+    return None
+
+
+def hbm_peak_gbs() -> tuple[float, str]:
+    try:
+        mp = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+        return float(mp["hbm_gbs"]), "measured copy bandwidth (MEASURED_PEAKS.json hbm_gbs)"
+    except Exception:
+        return 6800.0, "fallback 6.8 TB/s (no MEASURED_PEAKS.json)"
+
+
+def moment_roofline(t2: float, points_2d: int) -> dict:
+    """Roofline of the 2-D strip-moment kernels (strip extents, moment
+    prefix sums, per-target range sums): algorithmic HBM bytes over their
+    CUDA-event time, against the measured copy bandwidth. They are bound by
+    load latency (binary-search probes, 128-bit moment rows from L1/L2), not
+    by HBM; the committed ncu summary gives the issue rate they reach."""
+    peak, note = hbm_peak_gbs()
+    achieved = MOMENT_BYTES_PER_POINT * points_2d / t2 / 1e9
+    prof = "moments2d_mi64x100k_ncu.md"
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak,
+            "traffic": profile_figure(prof, "dram_bytes_per_step"),
+            "kernel": "k_m2_* (2-D strip moments: k_m2_density + prefix kernels)",
+            "bytes_per_point": MOMENT_BYTES_PER_POINT, "points_2d": points_2d,
+            "peak_kind": note,
+            "issue_frac_ncu": profile_figure(prof, "issue_frac"),
+            "note": "load-latency bound gather; see issue_frac_ncu and the profile"}
+
+
 def ncu_traffic() -> float | None:
     """DRAM bytes per launch of the 2-D pair kernel from the committed ncu
     summary (profiles/), if one has been captured."""
@@ -160,7 +208,7 @@ def cpu_port_sample(x: np.ndarray, h: np.ndarray, pairs, support):
     return support / dt, dt
 
 
-def compare_plain(ctx, x, ptr, log_fp64_pairs=2):
+def compare_plain(ctx, pctx, x, ptr, log_fp64_pairs=2):
     """Bandwidths by the AMISE search and then all-pairs MI, two ways:
     plain  -- the single-instance entry points called the way the reference
               calls them: per column 16 epa_convolution calls driven by the
@@ -168,6 +216,8 @@ def compare_plain(ctx, x, ptr, log_fp64_pairs=2):
               (per pair the 1-D marginal again and the 2-D joint, mi.cpp:37-59);
     batched+learned -- ent_hestimate_learned (features, network, warm search
               for all columns at once) and one ent_mi_all_pairs batch.
+    The plain side runs on its own context pctx with the library defaults
+    (the body each single call is fastest with), the batched side on ctx.
     Returns a dict of times, convolution counts and MI differences."""
     from entropical_gb300 import learned
     from entropical_gb300.densities import HEST_THUMB
@@ -176,19 +226,19 @@ def compare_plain(ctx, x, ptr, log_fp64_pairs=2):
     torch_sync = __import__("torch").cuda.synchronize
     torch_sync()
     t0 = time.perf_counter()
-    h0, _ = ctx.hestimate(x, HEST_THUMB)
+    h0, _ = pctx.hestimate(x, HEST_THUMB)
     h_plain, calls = np.zeros(M, np.float32), 0
     for j in range(M):
-        hj, c = hestimate_amise_plain(ctx, x[j], float(h0[j]))
+        hj, c = hestimate_amise_plain(pctx, x[j], float(h0[j]))
         h_plain[j], calls = hj, calls + c
     t_hest_plain = time.perf_counter() - t0
     t0 = time.perf_counter()
     mi_plain = np.zeros((M, M))
     for i in range(M):
-        Hi = -np.mean(np.log(ctx.combined_densities(x, None, [i], [h_plain[i]])))
+        Hi = -np.mean(np.log(pctx.combined_densities(x, None, [i], [h_plain[i]])))
         for j in range(i + 1, M):
-            Hj = -np.mean(np.log(ctx.combined_densities(x, None, [j], [h_plain[j]])))
-            Hij = -np.mean(np.log(ctx.combined_densities(x, None, [i, j],
+            Hj = -np.mean(np.log(pctx.combined_densities(x, None, [j], [h_plain[j]])))
+            Hij = -np.mean(np.log(pctx.combined_densities(x, None, [i, j],
                                                          [h_plain[i], h_plain[j]])))
             mi_plain[i, j] = mi_plain[j, i] = Hi + Hj - Hij
     t_mi_plain = time.perf_counter() - t0
@@ -229,14 +279,15 @@ def compare_plain(ctx, x, ptr, log_fp64_pairs=2):
     return out
 
 
-def compare_plain_te(ctx, n_coords=8, taus=(1, 5, 10)):
+def compare_plain_te(ctx, pctx, n_coords=8, taus=(1, 5, 10)):
     """Transfer entropy of all ordered pairs over the first n_coords of the
     coupled-Langevin data (200k frames, 3 lags), bandwidths by the AMISE
     search, two ways: plain -- per column 16 epa_convolution calls driven by
     the AmiseMin bracket logic, then one density call per density the TE
     estimates need (1-D, 2-D lagged, 2-D joint, 3-D; transs.cpp:39-115
     structure); batched+learned -- ent_hestimate_learned for all columns and
-    one ent_te_all_pairs batch for all pairs and lags."""
+    one ent_te_all_pairs batch for all pairs and lags. The plain side runs on
+    its own default context pctx."""
     from entropical_gb300 import learned, workloads
     from entropical_gb300.densities import HEST_THUMB
     from entropical_gb300.estimators import hestimate_amise_plain
@@ -246,25 +297,25 @@ def compare_plain_te(ctx, n_coords=8, taus=(1, 5, 10)):
     sync = __import__("torch").cuda.synchronize
     sync()
     t0 = time.perf_counter()
-    h0, _ = ctx.hestimate(x, HEST_THUMB)
-    hp = np.array([hestimate_amise_plain(ctx, x[j], float(h0[j]))[0] for j in range(M)],
+    h0, _ = pctx.hestimate(x, HEST_THUMB)
+    hp = np.array([hestimate_amise_plain(pctx, x[j], float(h0[j]))[0] for j in range(M)],
                   np.float32)
     calls, te_plain = 0, np.zeros((len(taus), M, M))
     for q, tau in enumerate(taus):
         n = N - tau
         xn = np.ascontiguousarray(x[:, :n])  # the n samples t of y_i and x_j
-        H1 = [-np.mean(np.log(ctx.combined_densities(xn, None, [i], [hp[i]])))
+        H1 = [-np.mean(np.log(pctx.combined_densities(xn, None, [i], [hp[i]])))
               for i in range(M)]
-        Hl = [-np.mean(np.log(ctx.combined_densities(x, None, [i, i], [hp[i], hp[i]], [tau, 0])))
+        Hl = [-np.mean(np.log(pctx.combined_densities(x, None, [i, i], [hp[i], hp[i]], [tau, 0])))
               for i in range(M)]
         calls += 2 * M
         for i in range(M):
             for j in range(M):
                 if i == j:
                     continue
-                H2 = -np.mean(np.log(ctx.combined_densities(xn, None, [i, j],
+                H2 = -np.mean(np.log(pctx.combined_densities(xn, None, [i, j],
                                                             [hp[i], hp[j]])))
-                H3 = -np.mean(np.log(ctx.combined_densities(
+                H3 = -np.mean(np.log(pctx.combined_densities(
                     x, None, [i, i, j], [hp[i], hp[i], hp[j]], [tau, 0, 0])))
                 calls += 2
                 te_plain[q, i, j] = H2 + Hl[i] - H3 - H1[i]
@@ -505,13 +556,21 @@ def main():
 
     if rank != 0:
         return
-    peak, peak_note = fp32_peak_tflops(n_sms)
     t2 = statistics.mean(k2_ms) / 1e3
-    # symmetric bodies (4, 5) evaluate each unordered pair once and add it to
-    # both points: 12 flops (6 FMA-pipe cycles) per evaluated pair
-    fpp = 12 if var2 in (4, 5) else 10
-    achieved = fpp * statistics.mean(k2_pairs) / t2 / 1e12
-    traffic = ncu_traffic()
+    if var2 == 7:
+        roofline = moment_roofline(t2, M * (M - 1) // 2 * N_FRAMES)
+    else:
+        peak, peak_note = fp32_peak_tflops(n_sms)
+        # symmetric bodies (4, 5) evaluate each unordered pair once and add it
+        # to both points: 12 flops (6 FMA-pipe cycles) per evaluated pair
+        fpp = 12 if var2 in (4, 5) else 10
+        achieved = fpp * statistics.mean(k2_pairs) / t2 / 1e12
+        roofline = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                    "frac": achieved / peak, "traffic": ncu_traffic(),
+                    "kernel": (f"k_density_sym<2,{32 if var2 == 4 else 16}> (2-D symmetric "
+                               "pair kernel)" if var2 in (4, 5) else
+                               f"k_density<2,16,{var2}> (2-D pair kernel)"),
+                    "flops_per_pair": fpp, "peak_kind": peak_note}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -532,23 +591,19 @@ def main():
                 "ms_per_step": e2e},
         "gpu_launches": launches,
         "autotuned": tuned,
-        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": traffic,
-                     "kernel": (f"k_density_sym<2,{32 if var2 == 4 else 16}> (2-D symmetric "
-                                "pair kernel)" if var2 in (4, 5) else
-                                f"k_density<2,16,{var2}> (2-D pair kernel)"),
-                     "flops_per_pair": fpp, "peak_kind": peak_note},
+        "roofline": roofline,
     }
     if not args.no_compare and ws == 1:
+        pctx = Context(local)  # library defaults for the single-instance calls
         try:
-            line["batched_learned_vs_plain"] = compare_plain(ctx, x, ptr)
+            line["batched_learned_vs_plain"] = compare_plain(ctx, pctx, x, ptr)
         except Exception as exc:
             line["batched_learned_vs_plain"] = {"error": str(exc)[:300]}
-    if not args.no_compare and ws == 1:
         try:
-            line["te_batched_learned_vs_plain"] = compare_plain_te(ctx)
+            line["te_batched_learned_vs_plain"] = compare_plain_te(ctx, pctx)
         except Exception as exc:
             line["te_batched_learned_vs_plain"] = {"error": str(exc)[:300]}
+        pctx.close()
     if not args.no_extra and ws == 1:
         try:
             line["other_configs"] = other_configs(ctx)

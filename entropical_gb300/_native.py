@@ -38,7 +38,7 @@ class Tuning(C.Structure):
     """ent_tuning: pair-kernel tile shapes."""
     _fields_ = [("targets_per_warp", C.c_uint32 * 3), ("cells_per_h", C.c_uint32),
                 ("pair_variant", C.c_uint32), ("pair_variant_by_dim", C.c_uint32 * 3),
-                ("cells_per_h3", C.c_uint32)]
+                ("cells_per_h3", C.c_uint32), ("moment_cells_per_h", C.c_uint32)]
 
 
 class NativeError(RuntimeError):

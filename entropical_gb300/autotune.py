@@ -5,7 +5,9 @@ per warp R (tile = 4 R targets), cells per bandwidth S along dimension 1 of
 2-D strips (dimensions 1 and 2 of 3-D strips), and the pair body (0: packed sub/fma + min; 1: saturating FMA;
 2: saturating at 5 CTAs/SM; 3: as 2 with larger chunks; 4: symmetric, each
 unordered pair once, 4 warps of 32 targets; 5: symmetric, 8 warps of 16;
-6, d = 1 only: range sums from exact prefix sums, no pair loop).
+6, d = 1 only: range sums from exact prefix sums, no pair loop; 7, d = 2
+only: strip moments, exact moment prefix sums for the strips inside the
+support and pairs only on its edge).
 ``tune`` times every supported combination on a sample of the caller's own
 batch (the first few instances, device time of the pair kernel of that
 dimension) and keeps the fastest; results are cached in a JSON file keyed by
@@ -25,17 +27,20 @@ CANDIDATES = {
     1: [(8, 2, 0), (16, 2, 0), (16, 2, 1), (16, 2, 2), (16, 2, 3), (16, 2, 4), (16, 2, 5),
         (16, 2, 6)],
     2: [(8, 2, 0), (16, 1, 2), (16, 2, 0), (16, 2, 1), (16, 2, 2), (16, 2, 3),
-        (16, 1, 4), (16, 2, 4), (16, 2, 5)],
+        (16, 1, 4), (16, 2, 4), (16, 2, 5), (16, 4, 7), (16, 6, 7)],
     3: [(4, 1, 0), (8, 1, 0), (8, 1, 1), (8, 1, 2), (8, 2, 2), (8, 1, 3), (8, 1, 4), (8, 2, 4),
         (8, 2, 5)],
 }
 
 
 def _set(ctx: Context, tpw, d: int, s: int, pv) -> None:
-    # s: cells per bandwidth of the strips (dimension 1 for d = 2, dimensions
-    # 1 and 2 for d = 3; unused for d = 1)
+    # s: cells per bandwidth of the strips (dimension 1 for d = 2, the strips
+    # of the strip-moment body 7, dimensions 1 and 2 for d = 3; unused for
+    # d = 1)
     if d == 3:
         ctx.set_tuning(tpw, 0, pv, cells_per_h3=s)
+    elif d == 2 and pv[1] == 7:
+        ctx.set_tuning(tpw, 0, pv, moment_cells_per_h=s)
     else:
         ctx.set_tuning(tpw, s, pv)
 

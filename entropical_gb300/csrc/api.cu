@@ -68,6 +68,12 @@ void Arena::reset() {
   total_used = 0;
 }
 
+size_t Arena::spare() const {
+  size_t cap = 0;
+  for (const auto& b : blocks) cap += b.size;
+  return cap > total_used ? cap - total_used : 0;
+}
+
 void Arena::release() {
   for (auto& b : blocks) cudaFree(b.ptr);
   blocks.clear();
@@ -288,8 +294,30 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
     if (!density_variant_supported(d, c.tile_r[d - 1], v)) v = 0;
     if (pair_uses_acc(v) && (mode & DM_COUNT)) v = 2;
     var_d[d] = v;
-    sym_d[d] = pair_uses_acc(v);
   }
+  if (var_d[2] == PAIR_MOMENT && c.moment_auto) {
+    uint64_t pts2 = 0;
+    for (uint32_t i = 0; i < ni; ++i)
+      if (insts[i].d == 2) pts2 += insts[i].n;
+    if (pts2 < MOMENT_MIN_POINTS) var_d[2] = PAIR_SYM;
+  }
+  if (var_d[2] == PAIR_MOMENT) {
+    // The moment prefix sums take 128 B per 2-D point; where the device
+    // cannot hold them with room to spare, the symmetric pair body runs.
+    size_t need = 0;
+    for (uint32_t i = 0; i < ni; ++i)
+      if (insts[i].d == 2) need += moments2d_prefix_bytes(insts[i].n) + 8 * (size_t)insts[i].n;
+    const size_t want = need + (need >> 3);
+    if (want > c.arena.spare()) {  // the device query only when the arena lacks room
+      size_t free_b = 0, total_b = 0;
+      if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        cudaGetLastError();
+        free_b = 0;
+      }
+      if (want + ((size_t)1 << 30) > free_b + c.arena.spare()) var_d[2] = PAIR_SYM;
+    }
+  }
+  for (int d = 1; d <= 3; ++d) sym_d[d] = pair_uses_acc(var_d[d]);
   uint64_t sym_points = 0;
   for (int d = 1; d <= 3; ++d) {
     group_base[d] = slot;
@@ -317,7 +345,8 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
         prod_hg2 *= (double)s.h[j] * (double)I.g2[j];
       }
       I.perm0 = vvals + voff[s.view[0]];
-      I.S = s.d == 2 ? std::max(1u, std::min(4u, s.S))
+      I.S = s.d == 2 ? (var_d[2] == PAIR_MOMENT ? c.moment_cells
+                                                : std::max(1u, std::min(4u, s.S)))
                      : (s.d == 3 ? std::max(1u, std::min(2u, s.S3[0] ? s.S3[0] : c.strip_subdiv3))
                                  : 1u);
       I.S2 = s.d == 3 ? std::max(1u, std::min(2u, s.S3[1] ? s.S3[1] : c.strip_subdiv3)) : 1u;
@@ -457,6 +486,49 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
       hi[seg_inst[q]].skeys = rk + seg_off[q];
     }
   }
+  // 2-D instances on the strip-moment body: strip extents, moment prefix
+  // sums and target blocks
+  std::vector<Mom2D> m2;
+  std::vector<uint32_t> m2_blk;
+  uint32_t m2_chunks = 0, m2_blocks = 0, m2_max_n = 0, m2_max_strips = 1;
+  if (var_d[2] == PAIR_MOMENT) {
+    for (uint32_t i : order) {
+      if (hi[i].d != 2) continue;
+      Mom2D m;
+      m.pts = static_cast<const float2*>(hi[i].pts);
+      m.skeys = hi[i].skeys;
+      m.strip_start = hi[i].strip_start;
+      m.ybound = static_cast<float2*>(c.arena.alloc(8 * (size_t)hi[i].n_strips));
+      m.acc = hi[i].acc;
+      m.P = c.arena.alloc(moments2d_prefix_bytes(hi[i].n));
+      if (!m.ybound || !m.P) return c.fail(ENT_ERR_CUDA, "out of device memory");
+      m.n = hi[i].n;
+      m.n_strips = hi[i].n_strips;
+      m.S = hi[i].S;
+      m.g2[0] = hi[i].g2[0];
+      m.g2[1] = hi[i].g2[1];
+      m.chunk_base = m2_chunks;
+      m.blk_base = m2_blocks;
+      m2_chunks += moments2d_chunks(m.n);
+      m2_blocks += moments2d_blocks(m.n);
+      m2_max_n = std::max(m2_max_n, m.n);
+      m2_max_strips = std::max(m2_max_strips, m.n_strips);
+      m2.push_back(m);
+      m2_blk.push_back(m.blk_base);
+    }
+    if (m2.size() > 65535u) return c.fail(ENT_ERR_TOO_LARGE, "too many 2-D instances in one batch");
+  }
+  Mom2D* dm2 = nullptr;
+  uint32_t* dm2_blk = nullptr;
+  void* m2_tot = nullptr;
+  if (!m2.empty()) {
+    dm2 = arena_upload(c, m2, &e);
+    if (e != cudaSuccess) return c.cuda_fail(e, "upload 2-D moments");
+    dm2_blk = arena_upload(c, m2_blk, &e);
+    if (e != cudaSuccess) return c.cuda_fail(e, "upload 2-D blocks");
+    m2_tot = c.arena.alloc(128 * (size_t)m2_chunks);
+    if (!m2_tot) return c.fail(ENT_ERR_CUDA, "out of device memory");
+  }
   InstDev* di = arena_upload(c, hi, &e);
   if (e != cudaSuccess) return c.cuda_fail(e, "upload instances");
 
@@ -540,6 +612,10 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
       if (d == 1 && var_d[1] == PAIR_RANGE) {
         r = launch_range1d(st, dr1, (uint32_t)r1.size(), r1_max_n, dr1_blk, r1_blocks, r1_tot);
         launches += 3;
+      } else if (d == 2 && var_d[2] == PAIR_MOMENT) {
+        r = launch_moments2d(st, dm2, (uint32_t)m2.size(), m2_max_n, m2_max_strips, dm2_blk,
+                             m2_blocks, m2_tot);
+        launches += 4;
       } else {
         r = launch_density(st, d, c.tile_r[d - 1], var_d[d], tiles + group_base[d],
                            group_slots[d], di_sorted, wc + d, c.d_err, tile_ls + group_base[d],
@@ -744,19 +820,28 @@ int ent_set_tuning(ent_ctx* ctx, const ent_tuning* t) {
       return c->fail(ENT_ERR_ARG, "unsupported targets_per_warp");
   if (t->cells_per_h > 4) return c->fail(ENT_ERR_ARG, "cells_per_h must be 1..4");
   if (t->cells_per_h3 > 2) return c->fail(ENT_ERR_ARG, "cells_per_h3 must be 1..2");
+  if (t->moment_cells_per_h == 1 || t->moment_cells_per_h > 12)
+    return c->fail(ENT_ERR_ARG, "moment_cells_per_h must be 2..12");
   if (t->pair_variant > PAIR_SYM + 2) return c->fail(ENT_ERR_ARG, "pair_variant must be 0..6");
   for (int d = 0; d < 3; ++d)
-    if (t->pair_variant_by_dim[d] > (d == 0 ? PAIR_RANGE + 1 : PAIR_SYM + 2))
-      return c->fail(ENT_ERR_ARG, d == 0 ? "pair_variant_by_dim[0] must be 0..7"
-                                          : "pair_variant_by_dim[1..2] must be 0..6");
-  if (t->pair_variant)
+    if (t->pair_variant_by_dim[d] >
+        (d == 0 ? PAIR_RANGE + 1 : (d == 1 ? PAIR_MOMENT + 1 : PAIR_SYM + 2)) ||
+        (d == 1 && t->pair_variant_by_dim[d] == PAIR_RANGE + 1))
+      return c->fail(ENT_ERR_ARG, d == 0   ? "pair_variant_by_dim[0] must be 0..7"
+                                  : d == 1 ? "pair_variant_by_dim[1] must be 0..6 or 8"
+                                           : "pair_variant_by_dim[2] must be 0..6");
+  if (t->pair_variant) {
     for (int d = 0; d < 3; ++d) c->pair_variant[d] = (int)t->pair_variant - 1;
+    c->moment_auto = false;
+  }
+  if (t->pair_variant_by_dim[1]) c->moment_auto = false;
   for (int d = 0; d < 3; ++d)
     if (t->pair_variant_by_dim[d]) c->pair_variant[d] = (int)t->pair_variant_by_dim[d] - 1;
   for (int d = 1; d <= 3; ++d)
     if (t->targets_per_warp[d - 1]) c->tile_r[d - 1] = (int)t->targets_per_warp[d - 1];
   if (t->cells_per_h) c->strip_subdiv = t->cells_per_h;
   if (t->cells_per_h3) c->strip_subdiv3 = t->cells_per_h3;
+  if (t->moment_cells_per_h) c->moment_cells = t->moment_cells_per_h;
   return ENT_OK;
 }
 
@@ -766,6 +851,7 @@ int ent_get_tuning(const ent_ctx* ctx, ent_tuning* t) {
   for (int d = 0; d < 3; ++d) t->targets_per_warp[d] = (uint32_t)c->tile_r[d];
   t->cells_per_h = c->strip_subdiv;
   t->cells_per_h3 = c->strip_subdiv3;
+  t->moment_cells_per_h = c->moment_cells;
   t->pair_variant = (uint32_t)c->pair_variant[1] + 1;
   for (int d = 0; d < 3; ++d) t->pair_variant_by_dim[d] = (uint32_t)c->pair_variant[d] + 1;
   return ENT_OK;

@@ -23,6 +23,7 @@ struct Arena {
   void* alloc(size_t bytes);
   void reset();
   void release();
+  size_t spare() const;  // bytes left in the blocks already held
 };
 
 struct Ctx {
@@ -52,8 +53,14 @@ struct Ctx {
   int tile_r[3] = {16, 16, 8};  // targets per warp of the pair kernel, by d
   // pair body per dimension: 0 min-based, 1 saturating FMA, 2 saturating at
   // 5 CTAs/SM, 3 as 2 with larger chunks (fastest measured: 2, 2, 1)
-  // PAIR_RANGE for d = 1, PAIR_SYM for d = 2, 3 (engine.h)
-  int pair_variant[3] = {6, 4, 4};
+  // PAIR_RANGE for d = 1, PAIR_MOMENT for d = 2, PAIR_SYM for d = 3 (engine.h)
+  int pair_variant[3] = {6, 7, 4};
+  // While the 2-D body is the default: calls with fewer 2-D points than
+  // MOMENT_MIN_POINTS (a single density, small batches) use PAIR_SYM, whose
+  // work items fill the GPU where one thread per target cannot. An explicit
+  // choice (set_tuning, the autotuner) clears it.
+  bool moment_auto = true;
+  uint32_t moment_cells = 4;  // strips per bandwidth of PAIR_MOMENT (2..12)
   bool use_graphs = true;       // capture the batch kernel sequence in a CUDA graph
 
   // grid of a persistent kernel: resident CTAs per SM x SMs, capped by work

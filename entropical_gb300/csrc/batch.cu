@@ -311,17 +311,22 @@ struct TuneCand {
 
 // Candidate shapes per density dimension: pair body (ent_tuning numbering
 // minus one), targets per warp of the ordered bodies, cells per bandwidth
-// (dimension 1 for d = 2, dimensions 1 and 2 for d = 3).
+// (dimension 1 for d = 2, the strip-moment strips for PAIR_MOMENT,
+// dimensions 1 and 2 for d = 3).
 std::vector<TuneCand> tune_candidates(uint32_t d) {
   if (d == 1) return {{2, 16, 2}, {4, 16, 2}, {5, 16, 2}, {PAIR_RANGE, 16, 2}};
-  if (d == 2) return {{2, 16, 2}, {4, 16, 1}, {4, 16, 2}, {4, 16, 3}, {5, 16, 2}};
+  if (d == 2)
+    return {{2, 16, 2},           {4, 16, 1},           {4, 16, 2},          {4, 16, 3},
+            {5, 16, 2},           {PAIR_MOMENT, 16, 4}, {PAIR_MOMENT, 16, 6}};
   return {{1, 8, 1}, {2, 8, 1}, {4, 8, 1}, {4, 8, 2}, {5, 8, 1}};
 }
 
 void apply_choice(Ctx& c, uint32_t d, int variant, int tile_r, uint32_t cells) {
   c.pair_variant[d - 1] = variant;
+  if (d == 2) c.moment_auto = false;
   c.tile_r[d - 1] = tile_r;
-  if (d == 2) c.strip_subdiv = cells;
+  if (d == 2 && variant == PAIR_MOMENT) c.moment_cells = cells;
+  else if (d == 2) c.strip_subdiv = cells;
   if (d == 3) c.strip_subdiv3 = cells;
 }
 
@@ -346,8 +351,10 @@ int ent_autotune(ent_ctx* ctx, const ent_instance* sample, size_t n_sample, uint
   if (it != c.tune_cache.end() && !(flags & ENT_TUNE_FORCE)) {
     apply_choice(c, d, it->second.variant, it->second.tile_r, it->second.cells);
   } else {
-    const Ctx::TuneChoice keep{c.pair_variant[d - 1], c.tile_r[d - 1],
-                               d == 2 ? c.strip_subdiv : c.strip_subdiv3};
+    const Ctx::TuneChoice keep{
+        c.pair_variant[d - 1], c.tile_r[d - 1],
+        d == 2 ? (c.pair_variant[1] == PAIR_MOMENT ? c.moment_cells : c.strip_subdiv)
+               : c.strip_subdiv3};
     std::vector<double> h(n_sample);
     const uint32_t bflags = flags & ENT_BATCH_DEVICE_INPUT;
     float best = 0.f;

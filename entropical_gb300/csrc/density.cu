@@ -719,6 +719,7 @@ int density_variant_supported(int d, int r, int v) {
   if (v == 0) return density_r_supported(d, r);
   if (pair_is_sym(v)) return d >= 1 && d <= 3;  // own tile shape, sym_tile_r
   if (v == PAIR_RANGE) return d == 1;            // range sums: tiles only finish
+  if (v == PAIR_MOMENT) return d == 2;           // strip moments: the same
   return v >= 1 && v <= 3 && r == (d == 3 ? 8 : 16);
 }
 

@@ -111,7 +111,8 @@ cudaError_t launch_plan(cudaStream_t st, const InstDev* insts, uint32_t n_inst,
                         uint32_t n_slots, uint64_t* n_src_total);
 // v: pair body, 0 = min-based, 1 = saturating FMA (needs g^2 < 1), 2-3 as 1
 // with other occupancy / chunk sizes, 4-5 symmetric (PAIR_SYM; r ignored),
-// 6 range sums (PAIR_RANGE, d = 1; not launched through here)
+// 6 range sums (PAIR_RANGE, d = 1), 7 strip moments (PAIR_MOMENT, d = 2);
+// those two are not launched through here
 cudaError_t launch_density(cudaStream_t st, int d, int r, int v, const TileDesc* tiles,
                            uint32_t n_slots, const InstDev* insts,
                            uint32_t* work_counter, uint32_t* err,
@@ -141,8 +142,14 @@ __host__ __device__ constexpr bool pair_is_sym(int v) {
 // fixed-point prefix sums after two binary searches. It writes InstDev::acc
 // and is finished by launch_sym_finish like the symmetric bodies.
 constexpr int PAIR_RANGE = 6;
+// Pair body PAIR_MOMENT (d = 2 only, moments2d.cu): per target and strip,
+// the x-support is one index range; strips wholly inside the y-support are
+// summed from exact fixed-point moment prefix sums, the others pair by pair.
+// Writes InstDev::acc like PAIR_RANGE.
+constexpr int PAIR_MOMENT = 7;
+constexpr uint64_t MOMENT_MIN_POINTS = 2000000;  // default rule: see Ctx::moment_auto
 __host__ __device__ constexpr bool pair_uses_acc(int v) {
-  return pair_is_sym(v) || v == PAIR_RANGE;
+  return pair_is_sym(v) || v == PAIR_RANGE || v == PAIR_MOMENT;
 }
 int sym_tile_r(int d, int v);
 int sym_tile_targets(int d, int v);
@@ -161,6 +168,25 @@ size_t range1d_prefix_bytes(uint32_t n);
 // rs: 1-D instances in ascending blk_base; chunk_tot: 32 B per chunk
 cudaError_t launch_range1d(cudaStream_t st, const Range1D* rs, uint32_t n_inst, uint32_t max_n,
                            const uint32_t* blk_base, uint32_t n_blocks, void* chunk_tot);
+struct Mom2D {
+  const float2* pts;            // strip-major scaled points (InstDev::pts)
+  const uint32_t* skeys;        // strip of every sorted position
+  const uint32_t* strip_start;  // n_strips + 1
+  float2* ybound;               // per strip: smallest and largest scaled y
+  double* acc;                  // unscaled sums by sorted position
+  void* P;                      // (n + 1) x 8 moment prefix sums, 128-bit each
+  uint32_t n, n_strips, S;      // S: strips examined on each side
+  float g2[2];
+  uint32_t chunk_base;          // first prefix chunk of the instance
+  uint32_t blk_base;            // first target block of the instance
+};
+uint32_t moments2d_chunks(uint32_t n);
+uint32_t moments2d_blocks(uint32_t n);
+size_t moments2d_prefix_bytes(uint32_t n);
+// ms: 2-D instances in ascending blk_base; chunk_tot: 128 B per chunk
+cudaError_t launch_moments2d(cudaStream_t st, const Mom2D* ms, uint32_t n_inst, uint32_t max_n,
+                             uint32_t max_strips, const uint32_t* blk_base, uint32_t n_blocks,
+                             void* chunk_tot);
 cudaError_t launch_density_sym(cudaStream_t st, int d, int v, const TileDesc* tiles,
                                uint32_t n_slots, const InstDev* insts,
                                uint32_t* work_counter, uint32_t* err, int n_sms,

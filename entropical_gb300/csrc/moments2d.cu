@@ -1,0 +1,343 @@
+// Two-dimensional density sums from exact strip moments (pair body
+// PAIR_MOMENT).
+//
+// The 2-D density at target t is sum_s wx(t,s) wy(t,s) with
+// w = max(0, g^2 - d^2) per dimension in scaled units (the reference's
+// densities_2d loop, densities_omp.cpp:97-126, and density_2d.cuh). The
+// points are strip-major: strips of width h/S along dimension 1, sorted by
+// dimension 0 inside each strip. For one target and one strip:
+//  * the sources in x-support form one index range [l, r) of the strip,
+//    found by two binary searches with the pair kernels' own test
+//    fma(-d, d, g^2) > 0 (monotone in |d|);
+//  * if the strip's smallest and largest y both pass the y test, every
+//    source of the strip does (|fl(y - t_y)| lies between the two), and on
+//    [l, r) the sum is a polynomial in the sources' coordinates:
+//      sum (G1 - (TX - X)^2)(G2 - (TY - Y)^2)
+//        = sum_{a,b <= 2} c_a(TX) d_b(TY) M_ab,   M_ab = sum X^a Y^b,
+//    with X = x 2^23, Y = y 2^23 fixed point and G = g^2 2^46. The moments
+//    come from prefix sums over the strip-major order taken modulo 2^128;
+//    the identity holds in the integers, reduction modulo 2^128 is a ring
+//    map and the true value lies in (-2^124, 2^124), so the signed modular
+//    result IS the exact integer: no cancellation whatever the offset or
+//    spread of the data;
+//  * otherwise (the strip crosses the edge of the y-support, at most two
+//    strips per target) the pairs of [l, r) are evaluated one by one.
+// Fixed-point rounding of the coordinates (2^-23 g) changes a kernel value
+// by less than 2^-21 g^2 per dimension, far below the 1e-5 density bar.
+//
+// Output: InstDev::acc[k] (unscaled sums by sorted position), finished by
+// launch_sym_finish like the other accumulating bodies.
+#include <algorithm>
+
+#include "engine.h"
+#include "staging.cuh"  // FULL_MASK
+
+namespace ent {
+namespace {
+
+typedef unsigned __int128 u128;
+
+constexpr uint32_t M2_TB = 128;               // targets per block
+constexpr uint32_t M2_PT = 256;               // prefix threads per block
+constexpr uint32_t M2_E = 4;                  // prefix values per thread
+constexpr uint32_t M2_CHUNK = M2_PT * M2_E;   // prefix values per block
+constexpr int NM = 8;  // X, Y, X^2, XY, Y^2, X^2 Y, X Y^2, X^2 Y^2
+
+// round(v 2^F) modulo 2^128 (two's complement), v finite.
+template <int F>
+__device__ __forceinline__ u128 quant(float v) {
+  const uint32_t b = __float_as_uint(v);
+  const int e = (int)((b >> 23) & 0xffu);
+  if (e == 0) return 0;  // zero or subnormal
+  const uint64_t m = (uint64_t)((b & 0x7fffffu) | 0x800000u);
+  const int sh = e - 150 + F;
+  u128 q;
+  if (sh >= 128) {
+    q = 0;
+  } else if (sh >= 0) {
+    q = (u128)m << sh;
+  } else if (sh > -25) {
+    q = (u128)((m + (1ull << (-sh - 1))) >> (-sh));
+  } else {
+    q = 0;
+  }
+  return (b & 0x80000000u) ? (u128)0 - q : q;
+}
+
+__device__ __forceinline__ void moments(float2 p, u128 (&m)[NM]) {
+  const u128 X = quant<23>(p.x), Y = quant<23>(p.y);
+  const u128 X2 = X * X, Y2 = Y * Y;
+  m[0] = X;
+  m[1] = Y;
+  m[2] = X2;
+  m[3] = X * Y;
+  m[4] = Y2;
+  m[5] = X2 * Y;
+  m[6] = X * Y2;
+  m[7] = X2 * Y2;
+}
+
+__device__ __forceinline__ u128 shfl_up128(u128 v, int o) {
+  const unsigned long long lo = __shfl_up_sync(FULL_MASK, (unsigned long long)v, o);
+  const unsigned long long hi = __shfl_up_sync(FULL_MASK, (unsigned long long)(v >> 64), o);
+  return ((u128)hi << 64) | lo;
+}
+__device__ __forceinline__ u128 shfl_idx128(u128 v, int l) {
+  const unsigned long long lo = __shfl_sync(FULL_MASK, (unsigned long long)v, l);
+  const unsigned long long hi = __shfl_sync(FULL_MASK, (unsigned long long)(v >> 64), l);
+  return ((u128)hi << 64) | lo;
+}
+
+__device__ __forceinline__ double s128_to_double(u128 v) {
+  const bool neg = (v >> 127) != 0;
+  if (neg) v = (u128)0 - v;
+  const double d = __ull2double_rn((unsigned long long)(v >> 64)) * 18446744073709551616.0 +
+                   __ull2double_rn((unsigned long long)v);
+  return neg ? -d : d;
+}
+
+// y extent (smallest, largest scaled y) of every strip: one warp per strip
+__global__ void k_m2_ybounds(const Mom2D* __restrict__ ms) {
+  const Mom2D& M = ms[blockIdx.y];
+  const uint32_t s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (s >= M.n_strips) return;  // warp-uniform
+  const uint32_t a = M.strip_start[s], b = M.strip_start[s + 1];
+  float lo = 3.4e38f, hi = -3.4e38f;
+  for (uint32_t k = a + lane; k < b; k += 32) {
+    const float y = M.pts[k].y;
+    lo = fminf(lo, y);
+    hi = fmaxf(hi, y);
+  }
+  for (int o = 16; o; o >>= 1) {
+    lo = fminf(lo, __shfl_xor_sync(FULL_MASK, lo, o));
+    hi = fmaxf(hi, __shfl_xor_sync(FULL_MASK, hi, o));
+  }
+  if (lane == 0) M.ybound[s] = make_float2(lo, hi);
+}
+
+// Block scan helper: exclusive prefix of v (per thread) over the block, and
+// the block total; sw holds NM u128 per warp.
+__device__ __forceinline__ void block_scan8(u128 (&v)[NM], u128 (&excl)[NM],
+                                            u128 (*sw)[NM]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  u128 inc[NM];
+#pragma unroll
+  for (int m = 0; m < NM; ++m) inc[m] = v[m];
+  for (int o = 1; o < 32; o <<= 1) {
+#pragma unroll
+    for (int m = 0; m < NM; ++m) {
+      const u128 u = shfl_up128(inc[m], o);
+      if (lane >= o) inc[m] += u;
+    }
+  }
+  if (lane == 31)
+#pragma unroll
+    for (int m = 0; m < NM; ++m) sw[warp][m] = inc[m];
+  __syncthreads();
+#pragma unroll
+  for (int m = 0; m < NM; ++m) {
+    u128 base = inc[m] - v[m];
+    for (int w = 0; w < warp; ++w) base += sw[w][m];
+    excl[m] = base;
+  }
+}
+
+// chunk totals of the eight moments
+__global__ void __launch_bounds__(M2_PT)
+    k_m2_totals(const Mom2D* __restrict__ ms, u128* __restrict__ tot) {
+  __shared__ u128 sw[M2_PT / 32][NM];
+  const Mom2D& M = ms[blockIdx.y];
+  const uint64_t b0 = (uint64_t)blockIdx.x * M2_CHUNK;
+  if (b0 >= M.n) return;  // block-uniform
+  const uint64_t k0 = b0 + (uint64_t)threadIdx.x * M2_E;
+  u128 s[NM], ex[NM];
+#pragma unroll
+  for (int m = 0; m < NM; ++m) s[m] = 0;
+  for (uint32_t e = 0; e < M2_E; ++e)
+    if (k0 + e < M.n) {
+      u128 q[NM];
+      moments(M.pts[k0 + e], q);
+#pragma unroll
+      for (int m = 0; m < NM; ++m) s[m] += q[m];
+    }
+  block_scan8(s, ex, sw);
+  if (threadIdx.x == M2_PT - 1)
+#pragma unroll
+    for (int m = 0; m < NM; ++m) tot[NM * ((size_t)M.chunk_base + blockIdx.x) + m] = ex[m] + s[m];
+}
+
+// one warp per instance: exclusive scan of its chunk totals, in place
+__global__ void k_m2_chunks(const Mom2D* __restrict__ ms, uint32_t n_inst,
+                            u128* __restrict__ tot) {
+  const uint32_t q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (q >= n_inst) return;  // warp-uniform
+  const uint32_t nch = (ms[q].n + M2_CHUNK - 1) / M2_CHUNK;
+  u128* t = tot + NM * (size_t)ms[q].chunk_base;
+  for (int m = 0; m < NM; ++m) {
+    u128 run = 0;
+    for (uint32_t b = 0; b < nch; b += 32) {
+      const bool in = b + lane < nch;
+      const u128 v = in ? t[NM * (b + lane) + m] : (u128)0;
+      u128 inc = v;
+      for (int o = 1; o < 32; o <<= 1) {
+        const u128 u = shfl_up128(inc, o);
+        if (lane >= o) inc += u;
+      }
+      if (in) t[NM * (b + lane) + m] = run + inc - v;
+      run += shfl_idx128(inc, 31);
+    }
+  }
+}
+
+// P[k] = sum_{j<k} moments(pts[j]), k = 0..n
+__global__ void __launch_bounds__(M2_PT)
+    k_m2_write(const Mom2D* __restrict__ ms, const u128* __restrict__ off) {
+  __shared__ u128 sw[M2_PT / 32][NM];
+  const Mom2D& M = ms[blockIdx.y];
+  const uint64_t b0 = (uint64_t)blockIdx.x * M2_CHUNK;
+  if (b0 >= M.n) return;  // block-uniform
+  const uint64_t k0 = b0 + (uint64_t)threadIdx.x * M2_E;
+  u128 s[NM], run[NM];
+#pragma unroll
+  for (int m = 0; m < NM; ++m) s[m] = 0;
+  for (uint32_t e = 0; e < M2_E; ++e)
+    if (k0 + e < M.n) {
+      u128 q[NM];
+      moments(M.pts[k0 + e], q);
+#pragma unroll
+      for (int m = 0; m < NM; ++m) s[m] += q[m];
+    }
+  block_scan8(s, run, sw);
+  const u128* o = off + NM * ((size_t)M.chunk_base + blockIdx.x);
+#pragma unroll
+  for (int m = 0; m < NM; ++m) run[m] += o[m];
+  u128* P = static_cast<u128*>(M.P);
+  if (b0 == 0 && threadIdx.x == 0)
+#pragma unroll
+    for (int m = 0; m < NM; ++m) P[m] = 0;
+  for (uint32_t e = 0; e < M2_E; ++e)
+    if (k0 + e < M.n) {
+      u128 q[NM];
+      moments(M.pts[k0 + e], q);
+#pragma unroll
+      for (int m = 0; m < NM; ++m) {
+        run[m] += q[m];
+        P[NM * (k0 + e + 1) + m] = run[m];
+      }
+    }
+}
+
+__device__ __forceinline__ bool insup(float a, float b, float g2) {
+  const float d = __fsub_rn(a, b);
+  return __fmaf_rn(-d, d, g2) > 0.f;
+}
+
+// acc + wx wy for one source p of target t (x inside the support)
+__device__ __forceinline__ float pair_term(float2 p, float2 t, float g1, float g2, float acc) {
+  const float dx = __fsub_rn(p.x, t.x), dy = __fsub_rn(p.y, t.y);
+  const float wy = __saturatef(__fmaf_rn(-dy, dy, g2));
+  return __fmaf_rn(__fmaf_rn(-dx, dx, g1), wy, acc);
+}
+
+// one thread per target
+__global__ void __launch_bounds__(M2_TB, 8)
+    k_m2_density(const Mom2D* __restrict__ ms, uint32_t n_inst,
+                 const uint32_t* __restrict__ blk_base) {
+  const uint32_t g = blockIdx.x;
+  uint32_t lo = 0, hi = n_inst;
+  while (hi - lo > 1) {
+    const uint32_t m = (lo + hi) / 2;
+    if (blk_base[m] <= g) lo = m; else hi = m;
+  }
+  const Mom2D& M = ms[lo];
+  const uint32_t k = (g - M.blk_base) * M2_TB + threadIdx.x;
+  if (k >= M.n) return;
+  const float2* __restrict__ pts = M.pts;
+  const uint32_t* __restrict__ ss = M.strip_start;
+  const u128* __restrict__ P = static_cast<const u128*>(M.P);
+  const float2 t = pts[k];
+  const float g1 = M.g2[0], g2 = M.g2[1];
+  const uint32_t s = M.skeys[k];
+  const uint32_t s_lo = s >= M.S ? s - M.S : 0u;
+  const uint32_t s_hi = min(M.n_strips - 1, s + M.S);
+  const u128 TX = quant<23>(t.x), TY = quant<23>(t.y);
+  const u128 c0 = quant<46>(g1) - TX * TX, c1 = TX + TX;
+  const u128 d0 = quant<46>(g2) - TY * TY, d1 = TY + TY;
+  u128 ex = 0;
+  double fs = 0.0;
+  for (uint32_t sp = s_lo; sp <= s_hi; ++sp) {
+    const uint32_t a = ss[sp], b = ss[sp + 1];
+    if (a == b) continue;
+    const float2 yb = M.ybound[sp];
+    const bool in_lo = insup(yb.x, t.y, g2), in_hi = insup(yb.y, t.y, g2);
+    if ((!in_lo && yb.x >= t.y) || (!in_hi && yb.y <= t.y)) continue;  // all out
+    // x-support range [l, r) of the strip
+    uint32_t l = a, r = b;
+    while (l < r) {
+      const uint32_t m = l + ((r - l) >> 1);
+      const float xm = pts[m].x;
+      if (xm < t.x && !insup(xm, t.x, g1)) l = m + 1; else r = m;
+    }
+    r = b;
+    uint32_t e = l;
+    while (e < r) {
+      const uint32_t m = e + ((r - e) >> 1);
+      const float xm = pts[m].x;
+      if (xm > t.x && !insup(xm, t.x, g1)) r = m; else e = m + 1;
+    }
+    r = e;
+    if (l >= r) continue;
+    if (in_lo && in_hi) {
+      const u128* pl = P + NM * (size_t)l;
+      const u128* pr = P + NM * (size_t)r;
+      u128 mo[NM];
+#pragma unroll
+      for (int m = 0; m < NM; ++m) mo[m] = pr[m] - pl[m];
+      const u128 cnt = (u128)(r - l);
+      // sum_b d_b M_ab for a = 0, 1, 2 (d_2 = -1), then sum_a c_a (.) (c_2 = -1)
+      const u128 e0 = d0 * cnt + d1 * mo[1] - mo[4];
+      const u128 e1 = d0 * mo[0] + d1 * mo[3] - mo[6];
+      const u128 e2 = d0 * mo[2] + d1 * mo[5] - mo[7];
+      ex += c0 * e0 + c1 * e1 - e2;
+    } else {
+      // four independent chains keep four loads in flight
+      float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+      uint32_t j = l;
+      for (; j + 4 <= r; j += 4) {
+        const float2 p0 = pts[j], p1 = pts[j + 1], p2 = pts[j + 2], p3 = pts[j + 3];
+        a0 = pair_term(p0, t, g1, g2, a0);
+        a1 = pair_term(p1, t, g1, g2, a1);
+        a2 = pair_term(p2, t, g1, g2, a2);
+        a3 = pair_term(p3, t, g1, g2, a3);
+      }
+      for (; j < r; ++j) a0 = pair_term(pts[j], t, g1, g2, a0);
+      fs += (double)((a0 + a1) + (a2 + a3));
+    }
+  }
+  // 2^-92 converts the fixed-point products back to units of g^4
+  M.acc[k] = s128_to_double(ex) * 0x1p-92 + fs;
+}
+
+}  // namespace
+
+uint32_t moments2d_chunks(uint32_t n) { return (n + M2_CHUNK - 1) / M2_CHUNK; }
+uint32_t moments2d_blocks(uint32_t n) { return (n + M2_TB - 1) / M2_TB; }
+size_t moments2d_prefix_bytes(uint32_t n) { return (size_t)NM * 16 * ((size_t)n + 1); }
+
+cudaError_t launch_moments2d(cudaStream_t st, const Mom2D* ms, uint32_t n_inst, uint32_t max_n,
+                             uint32_t max_strips, const uint32_t* blk_base, uint32_t n_blocks,
+                             void* chunk_tot) {
+  if (n_inst == 0 || n_blocks == 0) return cudaSuccess;
+  u128* tot = static_cast<u128*>(chunk_tot);
+  k_m2_ybounds<<<dim3((max_strips + 7) / 8, n_inst), 256, 0, st>>>(ms);
+  const dim3 gc(moments2d_chunks(std::max(max_n, 1u)), n_inst);
+  k_m2_totals<<<gc, M2_PT, 0, st>>>(ms, tot);
+  k_m2_chunks<<<(n_inst + 3) / 4, 128, 0, st>>>(ms, n_inst, tot);
+  k_m2_write<<<gc, M2_PT, 0, st>>>(ms, tot);
+  k_m2_density<<<n_blocks, M2_TB, 0, st>>>(ms, n_inst, blk_base);
+  return cudaGetLastError();
+}
+
+}  // namespace ent

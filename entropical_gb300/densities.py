@@ -144,22 +144,27 @@ class Context:
         t = _native.Tuning()
         self.check(self._lib.ent_get_tuning(self._h, C.byref(t)))
         return {"targets_per_warp": list(t.targets_per_warp), "cells_per_h": t.cells_per_h,
-                "cells_per_h3": t.cells_per_h3, "pair_variant": t.pair_variant - 1,
+                "cells_per_h3": t.cells_per_h3, "moment_cells_per_h": t.moment_cells_per_h,
+                "pair_variant": t.pair_variant - 1,
                 "pair_variant_by_dim": [v - 1 for v in t.pair_variant_by_dim]}
 
     def set_tuning(self, targets_per_warp=(0, 0, 0), cells_per_h: int = 0,
-                   pair_variant: int | None = None, cells_per_h3: int = 0) -> None:
+                   pair_variant: int | None = None, cells_per_h3: int = 0,
+                   moment_cells_per_h: int = 0) -> None:
         """Tile shapes and pair body (0 min-based, 1 saturating FMA, 2 the same at
         5 CTAs/SM, 3 as 2 with larger chunks, 4 symmetric with 4 warps of 32
         targets, 5 symmetric with 8 warps of 16) for every dimension, or a list
         of three per-dimension bodies (the first may also be 6: 1-D range sums
-        from exact prefix sums, the default for d = 1); cells per bandwidth of
-        the strips for d = 2 (1..4) and d = 3 (1..2); 0/None keeps."""
+        from exact prefix sums, the default for d = 1; the second 7: 2-D strip
+        moments, the default for d = 2); cells per bandwidth of the strips of
+        the pair bodies for d = 2 (1..4) and d = 3 (1..2), and of the strip
+        moments (2..12); 0/None keeps."""
         t = _native.Tuning()
         for i, v in enumerate(targets_per_warp):
             t.targets_per_warp[i] = int(v)
         t.cells_per_h = int(cells_per_h)
         t.cells_per_h3 = int(cells_per_h3)
+        t.moment_cells_per_h = int(moment_cells_per_h)
         if isinstance(pair_variant, (list, tuple)):
             for i, v in enumerate(pair_variant):
                 t.pair_variant_by_dim[i] = 0 if v is None else int(v) + 1

@@ -75,17 +75,25 @@ typedef struct {
                                    3 instead; own tiles of 128/128/64
                                    targets), 6 = as 5 with tiles of
                                    64/64/32 targets; default 5 for
-                                   dimensions 2 and 3 (get reports
-                                   dimension 2) */
+                                   dimension 3 (get reports dimension 2) */
   uint32_t pair_variant_by_dim[3]; /* the same per dimension (0 = keep);
                                       applied after pair_variant; for
                                       dimension 1 also 7 = range sums (no
                                       pair loop: each target's support is
                                       one range of the value-sorted points,
                                       summed from exact fixed-point prefix
-                                      sums), the default for d = 1 */
+                                      sums), the default for d = 1; for
+                                      dimension 2 also 8 = strip moments
+                                      (strips of h/4 inside a target's
+                                      support summed from exact moment
+                                      prefix sums, pairs only on its edge;
+                                      the symmetric body runs instead when
+                                      the device lacks the 128 B per point),
+                                      the default for d = 2 */
   uint32_t cells_per_h3;        /* d=3 strips: cells per bandwidth along
                                    dimensions 1 and 2, 1..2 (default 1) */
+  uint32_t moment_cells_per_h;  /* d=2 strip-moment body: strips per
+                                   bandwidth, 2..12 (default 4) */
 } ent_tuning;
 
 /* Context lifecycle. device < 0 selects the current device. */

@@ -27,6 +27,11 @@ def test_tune_and_apply(tmp_path, monkeypatch):
         assert ctx2.tuning()["pair_variant_by_dim"][1] == choice["pair_variant"]
 
 
+def _cells2(t):
+    # the 2-D strip count the chosen body uses
+    return t["moment_cells_per_h"] if t["pair_variant_by_dim"][1] == 7 else t["cells_per_h"]
+
+
 def test_native_autotuner_cache():
     """ent_autotune: the context's own tuner picks a shape per dimension on a
     sample batch, caches it per (d, size bucket), and results stay the same."""
@@ -42,11 +47,11 @@ def test_native_autotuner_cache():
         picks = {}
         for d in (1, 2, 3):
             t = ctx.autotune(sample, d)
-            assert 0 <= t["pair_variant_by_dim"][d - 1] <= (6 if d == 1 else 5)
-            picks[d] = (t["pair_variant_by_dim"][d - 1], t["cells_per_h"], t["cells_per_h3"])
+            assert 0 <= t["pair_variant_by_dim"][d - 1] <= {1: 6, 2: 7, 3: 5}[d]
+            picks[d] = (t["pair_variant_by_dim"][d - 1], _cells2(t), t["cells_per_h3"])
         assert ctx.autotune_cache_size() == 3
         ctx.set_tuning(pair_variant=0, cells_per_h=4, cells_per_h3=2)
         t2 = ctx.autotune(sample, 2)  # cached: applied again without timing
-        assert t2["pair_variant_by_dim"][1] == picks[2][0] and t2["cells_per_h"] == picks[2][1]
+        assert t2["pair_variant_by_dim"][1] == picks[2][0] and _cells2(t2) == picks[2][1]
         assert ctx.autotune_cache_size() == 3
         assert np.allclose(ctx.entropy_batch(sample), ref, rtol=0, atol=2e-6)
