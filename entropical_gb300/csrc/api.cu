@@ -372,13 +372,21 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
       }
       I.n_strips = I.ncell1 * I.ncell2;
       max_strips = std::max(max_strips, I.n_strips);
-      I.tt = (uint32_t)(sym_d[d] ? sym_tile_targets(d, var_d[d])
-                                 : density_tile_targets((int)s.d, c.tile_r[s.d - 1]));
-      I.tile_cap = (s.n + I.tt - 1) / I.tt + std::min(I.n_strips, s.n);  // tiles
       I.scale = (mode & DM_COUNT) ? 1.0 : std::pow(0.75, (double)s.d) / (s.norm * prod_hg2);
       I.out = s.out;
-      I.sym = sym_d[d] ? 1u : 0u;
-      if (I.sym) sym_points += s.n;
+      if (d == 2 && var_d[2] == PAIR_MOMENT) {
+        // one slot per block of targets of the moment kernel, which runs its
+        // own epilogue: no tiles, no FP64 accumulator
+        I.fused = 1;
+        I.tt = moments2d_block_targets();
+        I.tile_cap = (s.n + I.tt - 1) / I.tt;
+      } else {
+        I.tt = (uint32_t)(sym_d[d] ? sym_tile_targets(d, var_d[d])
+                                   : density_tile_targets((int)s.d, c.tile_r[s.d - 1]));
+        I.tile_cap = (s.n + I.tt - 1) / I.tt + std::min(I.n_strips, s.n);  // tiles
+        I.sym = sym_d[d] ? 1u : 0u;
+        if (I.sym) sym_points += s.n;
+      }
     }
     // Work items: a batch with few tiles for the persistent grid (a single
     // density, say) splits every tile's sources into up to 8 shares so that
@@ -499,7 +507,10 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
       m.skeys = hi[i].skeys;
       m.strip_start = hi[i].strip_start;
       m.ybound = static_cast<float2*>(c.arena.alloc(8 * (size_t)hi[i].n_strips));
-      m.acc = hi[i].acc;
+      m.perm = hi[i].perm;
+      m.out = hi[i].out;
+      m.scale = hi[i].scale;
+      m.slot_base = hi[i].tile_base;
       m.P = c.arena.alloc(moments2d_prefix_bytes(hi[i].n));
       if (!m.ybound || !m.P) return c.fail(ENT_ERR_CUDA, "out of device memory");
       m.n = hi[i].n;
@@ -614,7 +625,7 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
         launches += 3;
       } else if (d == 2 && var_d[2] == PAIR_MOMENT) {
         r = launch_moments2d(st, dm2, (uint32_t)m2.size(), m2_max_n, m2_max_strips, dm2_blk,
-                             m2_blocks, m2_tot);
+                             m2_blocks, m2_tot, c.d_logtab, tile_ls, mode);
         launches += 4;
       } else {
         r = launch_density(st, d, c.tile_r[d - 1], var_d[d], tiles + group_base[d],
@@ -625,7 +636,7 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
       rec(c.ev_d[d - 1][1]);
       c.ran_d[d - 1] = true;
       launches += 1;
-      if (sym_d[d]) {
+      if (sym_d[d] && !(d == 2 && var_d[2] == PAIR_MOMENT)) {
         r = launch_sym_finish(st, tiles + group_base[d], group_slots[d], di_sorted, c.d_logtab,
                               tile_ls + group_base[d], mode);
         if (r != cudaSuccess) return r;

@@ -69,6 +69,9 @@ struct InstDev {
   uint32_t parts;           // work items per tile (source runs split; 0 = 1);
                             // tile_cap counts work-item slots
   double* acc;              // symmetric mode: unscaled sums by sorted position
+  uint32_t fused;           // 1: a kernel with its own epilogue (strip moments)
+                            // owns the slots; the plan leaves them empty
+  uint32_t pad2;
 };
 
 struct TileDesc {
@@ -173,20 +176,26 @@ struct Mom2D {
   const uint32_t* skeys;        // strip of every sorted position
   const uint32_t* strip_start;  // n_strips + 1
   float2* ybound;               // per strip: smallest and largest scaled y
-  double* acc;                  // unscaled sums by sorted position
   void* P;                      // (n + 1) x 8 moment prefix sums, 128-bit each
+  const uint32_t* perm;         // original index of every sorted position
+  double* out;                  // per-point density by original index (nullable)
+  double scale;                 // InstDev::scale
   uint32_t n, n_strips, S;      // S: strips examined on each side
   float g2[2];
   uint32_t chunk_base;          // first prefix chunk of the instance
   uint32_t blk_base;            // first target block of the instance
+  uint32_t slot_base;           // first tile_logsum slot (one per target block)
 };
 uint32_t moments2d_chunks(uint32_t n);
 uint32_t moments2d_blocks(uint32_t n);
 size_t moments2d_prefix_bytes(uint32_t n);
-// ms: 2-D instances in ascending blk_base; chunk_tot: 128 B per chunk
+// ms: 2-D instances in ascending blk_base; chunk_tot: 128 B per chunk;
+// mode: the DM_* epilogue (no DM_COUNT)
 cudaError_t launch_moments2d(cudaStream_t st, const Mom2D* ms, uint32_t n_inst, uint32_t max_n,
                              uint32_t max_strips, const uint32_t* blk_base, uint32_t n_blocks,
-                             void* chunk_tot);
+                             void* chunk_tot, const double2* logtab, double* tile_logsum,
+                             uint32_t mode);
+uint32_t moments2d_block_targets();  // targets per block (= per tile slot)
 cudaError_t launch_density_sym(cudaStream_t st, int d, int v, const TileDesc* tiles,
                                uint32_t n_slots, const InstDev* insts,
                                uint32_t* work_counter, uint32_t* err, int n_sms,

@@ -25,8 +25,9 @@
 // Fixed-point rounding of the coordinates (2^-23 g) changes a kernel value
 // by less than 2^-21 g^2 per dimension, far below the 1e-5 density bar.
 //
-// Output: InstDev::acc[k] (unscaled sums by sorted position), finished by
-// launch_sym_finish like the other accumulating bodies.
+// The epilogue (scale, per-point output, FP64 log and per-block sums) runs
+// in the same kernel; the tile plan and the finish kernel are skipped for
+// these instances.
 #include <algorithm>
 
 #include "engine.h"
@@ -241,19 +242,8 @@ __device__ __forceinline__ float pair_term(float2 p, float2 t, float g1, float g
   return __fmaf_rn(__fmaf_rn(-dx, dx, g1), wy, acc);
 }
 
-// one thread per target
-__global__ void __launch_bounds__(M2_TB, 8)
-    k_m2_density(const Mom2D* __restrict__ ms, uint32_t n_inst,
-                 const uint32_t* __restrict__ blk_base) {
-  const uint32_t g = blockIdx.x;
-  uint32_t lo = 0, hi = n_inst;
-  while (hi - lo > 1) {
-    const uint32_t m = (lo + hi) / 2;
-    if (blk_base[m] <= g) lo = m; else hi = m;
-  }
-  const Mom2D& M = ms[lo];
-  const uint32_t k = (g - M.blk_base) * M2_TB + threadIdx.x;
-  if (k >= M.n) return;
+// Unscaled density sum of sorted position k of instance M (see the top).
+__device__ __forceinline__ double target_sum(const Mom2D& M, uint32_t k) {
   const float2* __restrict__ pts = M.pts;
   const uint32_t* __restrict__ ss = M.strip_start;
   const u128* __restrict__ P = static_cast<const u128*>(M.P);
@@ -317,18 +307,57 @@ __global__ void __launch_bounds__(M2_TB, 8)
     }
   }
   // 2^-92 converts the fixed-point products back to units of g^4
-  M.acc[k] = s128_to_double(ex) * 0x1p-92 + fs;
+  return s128_to_double(ex) * 0x1p-92 + fs;
+}
+
+// One thread per target, with the epilogue of the other bodies' finish
+// kernel fused: density = scale x sum, written by original index and/or
+// logged (FP64) and summed per block of targets in a fixed order; the
+// block sums land in the instance's slots of tile_logsum.
+__global__ void __launch_bounds__(M2_TB, 8)
+    k_m2_density(const Mom2D* __restrict__ ms, uint32_t n_inst,
+                 const uint32_t* __restrict__ blk_base, const double2* __restrict__ logtab,
+                 double* __restrict__ tile_logsum, uint32_t mode) {
+  __shared__ double s_part[M2_TB / 32];
+  const uint32_t g = blockIdx.x;
+  uint32_t lo = 0, hi = n_inst;
+  while (hi - lo > 1) {
+    const uint32_t m = (lo + hi) / 2;
+    if (blk_base[m] <= g) lo = m; else hi = m;
+  }
+  const Mom2D& M = ms[lo];
+  const uint32_t blk = g - M.blk_base;
+  const uint32_t k = blk * M2_TB + threadIdx.x;
+  double v = 0.0;  // this target's term of the block sum
+  if (k < M.n) {
+    const double dens = M.scale * target_sum(M, k);
+    if (mode & DM_WRITE_F64) M.out[M.perm[k]] = dens;
+    if (mode & DM_LOGSUM) v = log_fp64(dens, logtab);
+    else if (mode & DM_SUMV) v = dens;
+  }
+  if (mode & (DM_LOGSUM | DM_SUMV)) {  // block-uniform
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(FULL_MASK, v, o);
+    if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (uint32_t w = 0; w < M2_TB / 32; ++w) t += s_part[w];
+      tile_logsum[M.slot_base + blk] = t;
+    }
+  }
 }
 
 }  // namespace
 
 uint32_t moments2d_chunks(uint32_t n) { return (n + M2_CHUNK - 1) / M2_CHUNK; }
 uint32_t moments2d_blocks(uint32_t n) { return (n + M2_TB - 1) / M2_TB; }
+uint32_t moments2d_block_targets() { return M2_TB; }
 size_t moments2d_prefix_bytes(uint32_t n) { return (size_t)NM * 16 * ((size_t)n + 1); }
 
 cudaError_t launch_moments2d(cudaStream_t st, const Mom2D* ms, uint32_t n_inst, uint32_t max_n,
                              uint32_t max_strips, const uint32_t* blk_base, uint32_t n_blocks,
-                             void* chunk_tot) {
+                             void* chunk_tot, const double2* logtab, double* tile_logsum,
+                             uint32_t mode) {
   if (n_inst == 0 || n_blocks == 0) return cudaSuccess;
   u128* tot = static_cast<u128*>(chunk_tot);
   k_m2_ybounds<<<dim3((max_strips + 7) / 8, n_inst), 256, 0, st>>>(ms);
@@ -336,7 +365,7 @@ cudaError_t launch_moments2d(cudaStream_t st, const Mom2D* ms, uint32_t n_inst, 
   k_m2_totals<<<gc, M2_PT, 0, st>>>(ms, tot);
   k_m2_chunks<<<(n_inst + 3) / 4, 128, 0, st>>>(ms, n_inst, tot);
   k_m2_write<<<gc, M2_PT, 0, st>>>(ms, tot);
-  k_m2_density<<<n_blocks, M2_TB, 0, st>>>(ms, n_inst, blk_base);
+  k_m2_density<<<n_blocks, M2_TB, 0, st>>>(ms, n_inst, blk_base, logtab, tile_logsum, mode);
   return cudaGetLastError();
 }
 
