@@ -40,7 +40,7 @@ typedef unsigned __int128 u128;
 
 constexpr uint32_t M2_TB = 128;               // targets per block
 constexpr uint32_t M2_PT = 256;               // prefix threads per block
-constexpr uint32_t M2_E = 4;                  // prefix values per thread
+constexpr uint32_t M2_E = 8;                  // prefix values per thread
 constexpr uint32_t M2_CHUNK = M2_PT * M2_E;   // prefix values per block
 constexpr int NM = 8;  // X, Y, X^2, XY, Y^2, X^2 Y, X Y^2, X^2 Y^2
 
@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(M2_PT)
   const uint64_t b0 = (uint64_t)blockIdx.x * M2_CHUNK;
   if (b0 >= M.n) return;  // block-uniform
   const uint64_t k0 = b0 + (uint64_t)threadIdx.x * M2_E;
-  u128 s[NM], ex[NM];
+  u128 s[NM];
 #pragma unroll
   for (int m = 0; m < NM; ++m) s[m] = 0;
   for (uint32_t e = 0; e < M2_E; ++e)
@@ -162,10 +162,23 @@ __global__ void __launch_bounds__(M2_PT)
 #pragma unroll
       for (int m = 0; m < NM; ++m) s[m] += q[m];
     }
-  block_scan8(s, ex, sw);
-  if (threadIdx.x == M2_PT - 1)
+  // block total: warp sums, then the warps in order
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-    for (int m = 0; m < NM; ++m) tot[NM * ((size_t)M.chunk_base + blockIdx.x) + m] = ex[m] + s[m];
+  for (int m = 0; m < NM; ++m) {
+    for (int o = 16; o; o >>= 1) {
+      const unsigned long long lo = __shfl_xor_sync(FULL_MASK, (unsigned long long)s[m], o);
+      const unsigned long long hi = __shfl_xor_sync(FULL_MASK, (unsigned long long)(s[m] >> 64), o);
+      s[m] += ((u128)hi << 64) | lo;
+    }
+    if (lane == 0) sw[warp][m] = s[m];
+  }
+  __syncthreads();
+  if (threadIdx.x < NM) {
+    u128 t = 0;
+    for (uint32_t w = 0; w < M2_PT / 32; ++w) t += sw[w][threadIdx.x];
+    tot[NM * ((size_t)M.chunk_base + blockIdx.x) + threadIdx.x] = t;
+  }
 }
 
 // one warp per instance: exclusive scan of its chunk totals, in place
@@ -314,7 +327,7 @@ __device__ __forceinline__ double target_sum(const Mom2D& M, uint32_t k) {
 // kernel fused: density = scale x sum, written by original index and/or
 // logged (FP64) and summed per block of targets in a fixed order; the
 // block sums land in the instance's slots of tile_logsum.
-__global__ void __launch_bounds__(M2_TB, 8)
+__global__ void __launch_bounds__(M2_TB, 10)
     k_m2_density(const Mom2D* __restrict__ ms, uint32_t n_inst,
                  const uint32_t* __restrict__ blk_base, const double2* __restrict__ logtab,
                  double* __restrict__ tile_logsum, uint32_t mode) {
