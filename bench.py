@@ -134,11 +134,12 @@ def fp32_peak_tflops(n_sms: int) -> tuple[float, str]:
                   "(no measured FP32 figure in MEASURED_PEAKS.json)")
 
 
-# Algorithmic HBM bytes per 2-D point of the strip-moment kernels (one MI
-# step): the point (8 B) read by the strip-extent, moment-total, prefix-write
-# and target kernels (4 x 8), the 128 B moment prefix row written once and
-# read at least once (2 x 128), the strip key (4) and the FP64 sum (8).
-MOMENT_BYTES_PER_POINT = 4 * 8 + 2 * 128 + 4 + 8
+# Compulsory HBM bytes per 2-D point of the strip-moment kernels (one MI
+# step, log-sum epilogue): the point (8 B) read by the strip-extent,
+# moment-total, prefix-write and target kernels (4 x 8), the 128 B moment
+# prefix row written once, the strip key and the original index (4 + 4).
+# The target kernel re-reads only the rows at range ends, mostly from L2.
+MOMENT_BYTES_PER_POINT = 4 * 8 + 128 + 4 + 4
 
 
 def profile_figure(name: str, key: str) -> float | None:
