@@ -120,3 +120,43 @@ def test_moment_variant_only_for_two_dimensions(ctx):
         ctx.set_tuning(pair_variant=[None, None, 7])
     with pytest.raises(NativeError):
         ctx.set_tuning(pair_variant=[None, 6, None])
+
+
+@pytest.mark.parametrize("name,kind,tau", [("mi", 1, 0), ("transs", 2, 3), ("kldiv", 5, 0)])
+def test_moments_reference_estimators(mctx, name, kind, tau):
+    """The reference's estimator formulas (per-point output epilogue of the
+    moment kernel) against the FP64 oracle, as for the pair bodies."""
+    x = workloads.mi_coords(4000, 5, seed=31)
+    h = workloads.scott_bandwidth(x, 2)
+    r = mctx.reference_estimator(x, h, kind, tau)
+    f, bnd = O.reference_estimator_fp64(x, h, name, tau, bound=True)
+    assert np.all(np.abs(r - f) <= 1e-6 * bnd + 1e-12)
+
+
+def test_moments_dens_all_2d(mctx):
+    """dens -D 2 (per-point output and the plain-sum epilogue) against FP64."""
+    x = workloads.mi_coords(3000, 4, seed=5)
+    h = workloads.scott_bandwidth(x, 2)
+    d2 = mctx.dens_all(x, h, 2)
+    pairs = [(i, j) for i in range(4) for j in range(i + 1, 4)]
+    assert d2.shape == (len(pairs), 3000)
+    for r, (i, j) in enumerate(pairs):
+        p = O.density_fp64(np.stack([x[i], x[j]]), [h[i], h[j]])
+        assert np.max(np.abs(d2[r] - p / p.sum()) / (p / p.sum())) < 1e-5
+    assert np.allclose(d2.sum(1), 1.0, rtol=1e-12)
+
+
+def test_moments_default_rule(ctx):
+    """Without an explicit choice, a call below 2 M 2-D points runs the
+    symmetric pair body and a larger batch the strip moments; both agree."""
+    x = workloads.mi_coords(40000, 12, seed=9)
+    h = workloads.scott_bandwidth(x, 2)
+    assert ctx.tuning()["pair_variant_by_dim"][1] == 7
+    small, _ = ctx.mi_all_pairs(x[:3], h[:3])       # 3 x 40k 2-D points
+    k_small = ctx.last_stats().kernel_launches
+    big, _ = ctx.mi_all_pairs(x, h)                 # 66 x 40k = 2.64 M 2-D points
+    k_big = ctx.last_stats().kernel_launches
+    assert k_big > k_small                           # the moment kernels launched
+    assert np.allclose(big[:3, :3], small, rtol=0, atol=2e-6)
+    for i, j in [(0, 1), (4, 11)]:
+        assert abs(big[i, j] - O.mi_fp64(x[i], x[j], h[i], h[j])) < 1e-6
