@@ -256,6 +256,7 @@ int sort_views(Ctx& c, const std::vector<ViewSpec>& views, SortedViews* out) {
     if (out->stats[v].nonfinite)
       return c.fail(ENT_ERR_NONFINITE, "non-finite coordinate in the selection");
   out->perm = vvals;
+  out->keys = vk;
   return ENT_OK;
 }
 
@@ -295,28 +296,66 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
     if (pair_uses_acc(v) && (mode & DM_COUNT)) v = 2;
     var_d[d] = v;
   }
-  if (var_d[2] == PAIR_MOMENT && c.moment_auto) {
+  // 2-D under PAIR_MOMENT: which instances the strip moments take. Chosen
+  // explicitly: all. By default: those with at least MOMENT_MIN_SUPPORT
+  // in-support neighbours per target (a sampled estimate on the sorted views),
+  // if they hold MOMENT_MIN_POINTS points together; the symmetric pair kernel
+  // takes the rest (it is faster on small supports and on small calls).
+  std::vector<char> fused(ni, 0);
+  if (var_d[2] == PAIR_MOMENT) {
     uint64_t pts2 = 0;
     for (uint32_t i = 0; i < ni; ++i)
       if (insts[i].d == 2) pts2 += insts[i].n;
-    if (pts2 < MOMENT_MIN_POINTS) var_d[2] = PAIR_SYM;
-  }
-  if (var_d[2] == PAIR_MOMENT) {
-    // The moment prefix sums take 128 B per 2-D point; where the device
-    // cannot hold them with room to spare, the symmetric pair body runs.
+    if (!c.moment_auto) {
+      for (uint32_t i = 0; i < ni; ++i) fused[i] = insts[i].d == 2;
+    } else if (pts2 >= MOMENT_MIN_POINTS) {
+      std::vector<SupportEst> se;
+      std::vector<uint32_t> se_inst;
+      for (uint32_t i = 0; i < ni; ++i) {
+        if (insts[i].d != 2) continue;
+        const InstSpec& q = insts[i];
+        se.push_back({sv.keys + voff[q.view[0]], vvals + voff[q.view[0]], views[q.view[1]].x,
+                      q.n, q.h[0], q.h[1]});
+        se_inst.push_back(i);
+      }
+      SupportEst* dse = arena_upload(c, se, &e);
+      if (e != cudaSuccess) return c.cuda_fail(e, "upload support estimate");
+      float* dest = static_cast<float*>(c.arena.alloc(4 * se.size()));
+      if (!dest) return c.fail(ENT_ERR_CUDA, "out of device memory");
+      std::vector<float> est(se.size());
+      e = launch_support_est(st, dse, (uint32_t)se.size(), dest);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(est.data(), dest, 4 * est.size(), cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) return c.cuda_fail(e, "support estimate");
+      c.stats.kernel_launches += 1;
+      uint64_t pts_m = 0;
+      for (size_t q = 0; q < se.size(); ++q)
+        if (est[q] >= MOMENT_MIN_SUPPORT) {
+          fused[se_inst[q]] = 1;
+          pts_m += insts[se_inst[q]].n;
+        }
+      if (pts_m < MOMENT_MIN_POINTS) std::fill(fused.begin(), fused.end(), 0);
+    }
+    // The moment prefix sums take 128 B per point; where the device cannot
+    // hold them with room to spare, the symmetric pair body runs.
     size_t need = 0;
     for (uint32_t i = 0; i < ni; ++i)
-      if (insts[i].d == 2) need += moments2d_prefix_bytes(insts[i].n) + 8 * (size_t)insts[i].n;
+      if (fused[i]) need += moments2d_prefix_bytes(insts[i].n) + 8 * (size_t)insts[i].n;
     const size_t want = need + (need >> 3);
-    if (want > c.arena.spare()) {  // the device query only when the arena lacks room
+    if (need && want > c.arena.spare()) {  // the device query only when the arena lacks room
       size_t free_b = 0, total_b = 0;
       if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
         cudaGetLastError();
         free_b = 0;
       }
-      if (want + ((size_t)1 << 30) > free_b + c.arena.spare()) var_d[2] = PAIR_SYM;
+      if (want + ((size_t)1 << 30) > free_b + c.arena.spare())
+        std::fill(fused.begin(), fused.end(), 0);
     }
+    if (std::find(fused.begin(), fused.end(), 1) == fused.end()) var_d[2] = PAIR_SYM;
   }
+  bool sym2 = false;  // a 2-D instance on the symmetric pair kernel
+  for (uint32_t i = 0; i < ni; ++i) sym2 = sym2 || (insts[i].d == 2 && !fused[i]);
   for (int d = 1; d <= 3; ++d) sym_d[d] = pair_uses_acc(var_d[d]);
   uint64_t sym_points = 0;
   for (int d = 1; d <= 3; ++d) {
@@ -345,7 +384,7 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
         prod_hg2 *= (double)s.h[j] * (double)I.g2[j];
       }
       I.perm0 = vvals + voff[s.view[0]];
-      I.S = s.d == 2 ? (var_d[2] == PAIR_MOMENT ? c.moment_cells
+      I.S = s.d == 2 ? (fused[i] ? c.moment_cells
                                                 : std::max(1u, std::min(4u, s.S)))
                      : (s.d == 3 ? std::max(1u, std::min(2u, s.S3[0] ? s.S3[0] : c.strip_subdiv3))
                                  : 1u);
@@ -374,14 +413,16 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
       max_strips = std::max(max_strips, I.n_strips);
       I.scale = (mode & DM_COUNT) ? 1.0 : std::pow(0.75, (double)s.d) / (s.norm * prod_hg2);
       I.out = s.out;
-      if (d == 2 && var_d[2] == PAIR_MOMENT) {
+      if (fused[i]) {
         // one slot per block of targets of the moment kernel, which runs its
         // own epilogue: no tiles, no FP64 accumulator
         I.fused = 1;
         I.tt = moments2d_block_targets();
         I.tile_cap = (s.n + I.tt - 1) / I.tt;
       } else {
-        I.tt = (uint32_t)(sym_d[d] ? sym_tile_targets(d, var_d[d])
+        // 2-D instances beside strip moments run the symmetric pair kernel
+        const int body = (d == 2 && var_d[2] == PAIR_MOMENT) ? PAIR_SYM : var_d[d];
+        I.tt = (uint32_t)(sym_d[d] ? sym_tile_targets(d, body)
                                    : density_tile_targets((int)s.d, c.tile_r[s.d - 1]));
         I.tile_cap = (s.n + I.tt - 1) / I.tt + std::min(I.n_strips, s.n);  // tiles
         I.sym = sym_d[d] ? 1u : 0u;
@@ -501,7 +542,7 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
   uint32_t m2_chunks = 0, m2_blocks = 0, m2_max_n = 0, m2_max_strips = 1;
   if (var_d[2] == PAIR_MOMENT) {
     for (uint32_t i : order) {
-      if (hi[i].d != 2) continue;
+      if (!fused[i]) continue;
       Mom2D m;
       m.pts = static_cast<const float2*>(hi[i].pts);
       m.skeys = hi[i].skeys;
@@ -624,9 +665,16 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
         r = launch_range1d(st, dr1, (uint32_t)r1.size(), r1_max_n, dr1_blk, r1_blocks, r1_tot);
         launches += 3;
       } else if (d == 2 && var_d[2] == PAIR_MOMENT) {
+        // the moments take their instances, the symmetric kernel the rest
         r = launch_moments2d(st, dm2, (uint32_t)m2.size(), m2_max_n, m2_max_strips, dm2_blk,
                              m2_blocks, m2_tot, c.d_logtab, tile_ls, mode);
         launches += 4;
+        if (r == cudaSuccess && sym2) {
+          r = launch_density(st, 2, c.tile_r[1], PAIR_SYM, tiles + group_base[2],
+                             group_slots[2], di_sorted, wc + 2, c.d_err,
+                             tile_ls + group_base[2], mode, c.n_sms, &launched);
+          launches += 1;
+        }
       } else {
         r = launch_density(st, d, c.tile_r[d - 1], var_d[d], tiles + group_base[d],
                            group_slots[d], di_sorted, wc + d, c.d_err, tile_ls + group_base[d],
@@ -636,7 +684,7 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
       rec(c.ev_d[d - 1][1]);
       c.ran_d[d - 1] = true;
       launches += 1;
-      if (sym_d[d] && !(d == 2 && var_d[2] == PAIR_MOMENT)) {
+      if (sym_d[d] && (d != 2 || var_d[2] != PAIR_MOMENT || sym2)) {
         r = launch_sym_finish(st, tiles + group_base[d], group_slots[d], di_sorted, c.d_logtab,
                               tile_ls + group_base[d], mode);
         if (r != cudaSuccess) return r;

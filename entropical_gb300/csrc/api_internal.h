@@ -55,10 +55,12 @@ struct Ctx {
   // 5 CTAs/SM, 3 as 2 with larger chunks (fastest measured: 2, 2, 1)
   // PAIR_RANGE for d = 1, PAIR_MOMENT for d = 2, PAIR_SYM for d = 3 (engine.h)
   int pair_variant[3] = {6, 7, 4};
-  // While the 2-D body is the default: calls with fewer 2-D points than
-  // MOMENT_MIN_POINTS (a single density, small batches) use PAIR_SYM, whose
-  // work items fill the GPU where one thread per target cannot. An explicit
-  // choice (set_tuning, the autotuner) clears it.
+  // While the 2-D body is the default, the engine picks per instance: the
+  // strip moments for supports of at least MOMENT_MIN_SUPPORT neighbours per
+  // target when such instances hold MOMENT_MIN_POINTS points together, else
+  // PAIR_SYM (its work items fill the GPU where one thread per target cannot,
+  // and it is faster on small supports). An explicit choice (set_tuning, the
+  // autotuner) clears it: then every 2-D instance takes the moments.
   bool moment_auto = true;
   uint32_t moment_cells = 4;  // strips per bandwidth of PAIR_MOMENT (2..12)
   bool use_graphs = true;       // capture the batch kernel sequence in a CUDA graph
@@ -99,6 +101,7 @@ struct SortedViews {
   std::vector<ent::ViewStats> stats;
   std::vector<uint64_t> off;  // element offset of each view in perm
   uint32_t* perm = nullptr;   // device: per view, sorted local indices
+  uint32_t* keys = nullptr;   // device: per view, the sorted orderable keys
   uint32_t max_n = 0;
 };
 int sort_views(Ctx& c, const std::vector<ViewSpec>& views, SortedViews* out);

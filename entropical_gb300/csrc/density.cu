@@ -251,7 +251,7 @@ __global__ void k_plan(const InstDev* __restrict__ insts, uint32_t n_inst,
   const uint32_t t = (g - I.tile_base) / parts;
   td.part = (g - I.tile_base) % parts;
   const uint32_t total = I.tile_off[I.n_strips];
-  if (t >= total || I.fused) {
+  if (t >= total || I.fused) {  // strip-moment instances have no tiles
     tiles[g] = td;
     return;
   }

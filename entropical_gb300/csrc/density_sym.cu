@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(NW * 32, MINB)
         const TileDesc* T = tiles + g;
         const uint32_t nr = T->n_runs;
         s_tb = T->t_begin;
-        s_tc = T->t_count;
+        s_tc = insts[T->inst].fused ? 0u : T->t_count;  // moment-owned: skip
         s_inst = T->inst;
         s_nr = nr;
         run_pre[0] = 0;
@@ -311,6 +311,8 @@ __global__ void __launch_bounds__(256)
   const int lane = threadIdx.x & 31;
   if (g >= n_slots) return;  // warp-uniform
   const TileDesc& T = tiles[g];
+  // the strip-moment kernel writes the slots of the instances it owns
+  if (insts[T.inst].fused) return;  // warp-uniform
   const uint32_t tc = T.part == 0 ? T.t_count : 0u;  // one slot per tile finishes it
   double ls = 0.0;
   if (tc) {

@@ -69,8 +69,8 @@ struct InstDev {
   uint32_t parts;           // work items per tile (source runs split; 0 = 1);
                             // tile_cap counts work-item slots
   double* acc;              // symmetric mode: unscaled sums by sorted position
-  uint32_t fused;           // 1: a kernel with its own epilogue (strip moments)
-                            // owns the slots; the plan leaves them empty
+  uint32_t fused;           // 1: the strip-moment kernel owns this instance
+                            // (no tiles; pair kernel and finish skip it)
   uint32_t pad2;
 };
 
@@ -150,7 +150,14 @@ constexpr int PAIR_RANGE = 6;
 // summed from exact fixed-point moment prefix sums, the others pair by pair.
 // Writes InstDev::acc like PAIR_RANGE.
 constexpr int PAIR_MOMENT = 7;
-constexpr uint64_t MOMENT_MIN_POINTS = 2000000;  // default rule: see Ctx::moment_auto
+constexpr uint64_t MOMENT_MIN_POINTS = 1000000;  // default rule: see Ctx::moment_auto
+// Default rule per instance: the moments take a 2-D instance with at least
+// this many in-support neighbours per target (sampled estimate, within 15 %
+// of the true mean on the bench data). Measured: they win 1.5-5x at 19-23k
+// (MI, lagged TE pairs), about break even at 8.5k (joint TE pairs: 5 %
+// faster in the 32-coordinate batch, 10 % slower in an 8-coordinate one) and
+// lose 25 % at 3k (the uneven batch).
+constexpr float MOMENT_MIN_SUPPORT = 6000.f;
 __host__ __device__ constexpr bool pair_uses_acc(int v) {
   return pair_is_sym(v) || v == PAIR_RANGE || v == PAIR_MOMENT;
 }
@@ -191,10 +198,24 @@ uint32_t moments2d_blocks(uint32_t n);
 size_t moments2d_prefix_bytes(uint32_t n);
 // ms: 2-D instances in ascending blk_base; chunk_tot: 128 B per chunk;
 // mode: the DM_* epilogue (no DM_COUNT)
+// ms: 2-D instances in ascending blk_base; chunk_tot: 128 B per chunk;
+// mode: the DM_* epilogue (no DM_COUNT)
 cudaError_t launch_moments2d(cudaStream_t st, const Mom2D* ms, uint32_t n_inst, uint32_t max_n,
                              uint32_t max_strips, const uint32_t* blk_base, uint32_t n_blocks,
                              void* chunk_tot, const double2* logtab, double* tile_logsum,
                              uint32_t mode);
+// Mean in-support neighbours per target of 2-D instances, sampled: per
+// instance 32 targets at quantiles of dimension 0, each with its window
+// count in dimension 0 times the y-support fraction of up to 32 window points.
+struct SupportEst {
+  const uint32_t* keys0;  // dimension-0 sorted orderable keys of the instance
+  const uint32_t* perm0;  // their original indices
+  const float* y1;        // dimension-1 coordinates by original index
+  uint32_t n;
+  float h0, h1;
+};
+cudaError_t launch_support_est(cudaStream_t st, const SupportEst* in, uint32_t n_inst,
+                               float* est);
 uint32_t moments2d_block_targets();  // targets per block (= per tile slot)
 cudaError_t launch_density_sym(cudaStream_t st, int d, int v, const TileDesc* tiles,
                                uint32_t n_slots, const InstDev* insts,

@@ -26,8 +26,8 @@
 // by less than 2^-21 g^2 per dimension, far below the 1e-5 density bar.
 //
 // The epilogue (scale, per-point output, FP64 log and per-block sums) runs
-// in the same kernel; the tile plan and the finish kernel are skipped for
-// these instances.
+// in the same kernel; the tile plan leaves these instances without tiles and
+// the pair kernel and its finish skip them.
 #include <algorithm>
 
 #include "engine.h"
@@ -360,7 +360,49 @@ __global__ void __launch_bounds__(M2_TB, 10)
   }
 }
 
+// One warp per instance; lane l samples the target at quantile (2l+1)/64 of
+// dimension 0.
+__global__ void k_support_est(const SupportEst* __restrict__ in, uint32_t n_inst,
+                              float* __restrict__ est) {
+  const uint32_t q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (q >= n_inst) return;  // warp-uniform
+  const SupportEst& E = in[q];
+  const uint32_t n = E.n;
+  const uint32_t pos = (uint32_t)(((2ull * lane + 1) * n) / 64);
+  const float xt = key_float(E.keys0[pos]);
+  const float yt = E.y1[E.perm0[pos]];
+  // window [lo, hi) of dimension 0 within h0 of xt
+  uint32_t lo = 0, hi = n;
+  while (lo < hi) {
+    const uint32_t m = lo + ((hi - lo) >> 1);
+    if (key_float(E.keys0[m]) <= xt - E.h0) lo = m + 1; else hi = m;
+  }
+  uint32_t a = lo, b = n;
+  while (a < b) {
+    const uint32_t m = a + ((b - a) >> 1);
+    if (key_float(E.keys0[m]) < xt + E.h0) a = m + 1; else b = m;
+  }
+  const uint32_t c = a - lo;
+  const uint32_t ns = min(c, 32u);
+  uint32_t in_y = 0;
+  for (uint32_t s = 0; s < ns; ++s) {
+    const uint32_t p = lo + (uint32_t)(((uint64_t)s * c) / ns);
+    in_y += fabsf(E.y1[E.perm0[p]] - yt) < E.h1 ? 1u : 0u;
+  }
+  float k = ns ? (float)c * (float)in_y / (float)ns : 0.f;
+  for (int o = 16; o; o >>= 1) k += __shfl_xor_sync(FULL_MASK, k, o);
+  if (lane == 0) est[q] = k / 32.f;
+}
+
 }  // namespace
+
+cudaError_t launch_support_est(cudaStream_t st, const SupportEst* in, uint32_t n_inst,
+                               float* est) {
+  if (n_inst == 0) return cudaSuccess;
+  k_support_est<<<(n_inst + 3) / 4, 128, 0, st>>>(in, n_inst, est);
+  return cudaGetLastError();
+}
 
 uint32_t moments2d_chunks(uint32_t n) { return (n + M2_CHUNK - 1) / M2_CHUNK; }
 uint32_t moments2d_blocks(uint32_t n) { return (n + M2_TB - 1) / M2_TB; }

@@ -160,3 +160,27 @@ def test_moments_default_rule(ctx):
     assert np.allclose(big[:3, :3], small, rtol=0, atol=2e-6)
     for i, j in [(0, 1), (4, 11)]:
         assert abs(big[i, j] - O.mi_fp64(x[i], x[j], h[i], h[j])) < 1e-6
+
+
+def test_moments_mixed_batch_per_instance_choice(ctx):
+    """A default batch above 2 M 2-D points with instances of very different
+    support per target: the device picks the body per instance (moments for
+    wide supports, the symmetric pair kernel for narrow ones); entropies
+    match a symmetric-only context (itself checked against FP64 above)."""
+    from entropical_gb300 import Context
+    rng = np.random.default_rng(23)
+    items = []
+    for q in range(24):
+        n = 120_000
+        x = rng.standard_normal((2, n)).astype(np.float32)
+        if q % 2:
+            x = np.tanh(2.5 * x).astype(np.float32)   # concentrated: wide support
+            h = np.float32([0.3, 0.3])
+        else:
+            h = np.float32([0.02, 0.03])               # narrow support
+        items.append((x, h))
+    H = ctx.entropy_batch(items)
+    with Context(0) as s:
+        s.set_tuning(pair_variant=[None, 4, None])
+        Hs = s.entropy_batch(items)
+    assert np.max(np.abs(H - Hs)) < 2e-6
