@@ -88,8 +88,13 @@ typedef struct {
                                       support summed from exact moment
                                       prefix sums, pairs only on its edge;
                                       the symmetric body runs instead when
-                                      the device lacks the 128 B per point),
-                                      the default for d = 2 */
+                                      the device lacks the 128 B per point).
+                                      Default for d = 2: chosen per
+                                      instance, the moments for supports of
+                                      6,000+ neighbours per target (sampled
+                                      estimate), else the symmetric body;
+                                      setting 8 explicitly gives every 2-D
+                                      instance to the moments */
   uint32_t cells_per_h3;        /* d=3 strips: cells per bandwidth along
                                    dimensions 1 and 2, 1..2 (default 1) */
   uint32_t moment_cells_per_h;  /* d=2 strip-moment body: strips per
