@@ -4,17 +4,21 @@
 Workload (one step): all-pairs mutual information over 64 coordinates x
 100,000 frames -- 64 1-D marginal densities and 2,016 2-D joint densities,
 Scott-rule bandwidths, resubstitution MI -- computed as ONE batch through the
-library (one persistent pair-kernel launch per dimension). Synthetic, seeded
-data: x_t = tanh(A z_t), z a 16-dim AR(1) (phi 0.95), columns standardised.
+library (1-D range sums and 2-D strip moments by default, one launch
+sequence per dimension). Synthetic, seeded data: x_t = tanh(A z_t), z a
+16-dim AR(1) (phi 0.95), columns standardised.
 
-value      in-support pair-kernel evaluations per second, inputs resident in
-           HBM (ent_mi_all_pairs_device), device time on the library stream
+value      in-support pair-kernel evaluations per second (the step's work in
+           the reference's unit), inputs resident in HBM
+           (ent_mi_all_pairs_device), device time on the library stream
 e2e        same metric through the host-buffer C-ABI call ent_mi_all_pairs,
            host->device copy of the coordinates and device->host copy of the
            MI matrix inside the timed region
-roofline   the dominant kernel (2-D pair kernel) against the FP32 CUDA-core
-           peak: 10 flops per evaluated (target, candidate) pair, 12 for the
-           symmetric bodies (each evaluated pair also added to the source)
+roofline   the dominant 2-D kernels: for the strip moments, compulsory HBM
+           bytes over their time against the measured copy bandwidth (with
+           the issue fraction from the committed ncu summary); for a pair
+           body chosen with --pair-variant, 10 flops per evaluated pair (12
+           for the symmetric bodies) against the FP32 CUDA-core peak
 cpu_baseline  the reference's OpenMP density algorithm (restated in C with
            its own linear window scans, all host cores) on a bounded sample
 
