@@ -390,24 +390,27 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
                                  : 1u);
       I.S2 = s.d == 3 ? std::max(1u, std::min(2u, s.S3[1] ? s.S3[1] : c.strip_subdiv3)) : 1u;
       I.ncell1 = I.ncell2 = 1;
+      // Cells of width h/S, widened so that the FP32 cell index (cell_of:
+      // error below 1.8e-7 cells per cell of range) keeps two points within
+      // h at most S cells apart. Capping the cell count only merges far
+      // cells (more candidates, never fewer in-support sources).
+      auto cells = [](const ViewStats& v, float hh, uint32_t S, double cap, float* inv_w,
+                      uint32_t* ncell) {
+        const double range = (double)v.mx - (double)v.mn;
+        double w = (double)hh / S * (1.0 + 1e-4);
+        const double nc0 = std::min(std::floor(range / w) + 1.0, cap);
+        w = (double)hh / S * (1.0 + std::max(1e-4, 6e-7 * nc0 / S));
+        *inv_w = (float)(1.0 / w);
+        *ncell = (uint32_t)std::min(std::floor(range / w) + 1.0, cap);
+      };
       if (s.d >= 2) {
-        const ViewStats& a = vs[s.view[1]];
-        const double w = (double)s.h[1] / I.S * (1.0 + 1e-4);
-        I.lo1 = a.mn;
-        I.inv_w1 = 1.0 / w;
-        // Capping the cell count only merges far cells (more candidates,
-        // never fewer in-support sources).
-        I.ncell1 = (uint32_t)std::min<double>(
-            std::floor(((double)a.mx - (double)a.mn) / w) + 1.0,
-            s.d == 2 ? (1u << 16) : (1u << 10));
+        I.lo1 = vs[s.view[1]].mn;
+        cells(vs[s.view[1]], s.h[1], I.S, s.d == 2 ? (1u << 16) : (1u << 10), &I.inv_w1,
+              &I.ncell1);
       }
       if (s.d == 3) {
-        const ViewStats& b = vs[s.view[2]];
-        const double w = (double)s.h[2] / I.S2 * (1.0 + 1e-4);
-        I.lo2 = b.mn;
-        I.inv_w2 = 1.0 / w;
-        I.ncell2 = (uint32_t)std::min<double>(
-            std::floor(((double)b.mx - (double)b.mn) / w) + 1.0, 1u << 10);
+        I.lo2 = vs[s.view[2]].mn;
+        cells(vs[s.view[2]], s.h[2], I.S2, 1u << 10, &I.inv_w2, &I.ncell2);
       }
       I.n_strips = I.ncell1 * I.ncell2;
       max_strips = std::max(max_strips, I.n_strips);

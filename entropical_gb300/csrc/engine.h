@@ -52,7 +52,9 @@ struct InstDev {
   uint32_t ncell1, ncell2;  // cells along dims 1 and 2 (1 when absent)
   uint32_t tile_base, tile_cap;
   float lo1, lo2;           // cell-grid origins
-  double inv_w1, inv_w2;    // inverse cell widths (cell width = h/S, widened)
+  float inv_w1, inv_w2;     // inverse cell widths (cell width = h/S, widened so
+                            // that the FP32 cell index of k_strip_keys can
+                            // never put two points within h more than S apart)
   float sc[3];  // exact power-of-two scale 2^k_j with g_j = h_j 2^k_j in [0.5, 1)
   float g2[3];  // g_j^2: the support radius squared in scaled units
   const uint32_t* perm0;    // dimension-0 sorted order (view sort)
