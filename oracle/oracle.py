@@ -37,10 +37,19 @@ def build_oracle() -> Path:
     return ORACLE_SO
 
 
-def build_ref(reference: str = "/root/reference") -> Path | None:
-    if not Path(reference, "densities_omp.cpp").exists():
+def reference_dir() -> Path | None:
+    """The reference checkout: $ENT_REFERENCE, else a ``reference`` directory
+    beside this repository; None when neither holds the reference sources."""
+    env = os.environ.get("ENT_REFERENCE")
+    cand = Path(env) if env else HERE.parent.parent / "reference"
+    return cand if (cand / "densities_omp.cpp").exists() else None
+
+
+def build_ref(reference: str | Path | None = None) -> Path | None:
+    ref_dir = Path(reference) if reference else reference_dir()
+    if ref_dir is None or not (ref_dir / "densities_omp.cpp").exists():
         return None
-    subprocess.run(["make", "-s", "-j8", "-C", str(HERE), "ref", f"REF={reference}"], check=True)
+    subprocess.run(["make", "-s", "-j8", "-C", str(HERE), "ref", f"REF={ref_dir}"], check=True)
     return REF_SO
 
 

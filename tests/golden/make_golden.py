@@ -2,12 +2,13 @@
 
 The reference (lettis/entropical) ships no tests or golden vectors, so the
 fixtures are produced by running its OpenMP sources, compiled in place by
-``make -C oracle ref`` (needs the reference checkout, default
-/root/reference), on small seeded inputs. The committed fixtures let the
+``make -C oracle ref`` (needs the reference checkout: ``--reference``,
+$ENT_REFERENCE, or a ``reference`` directory beside this repository), on
+small seeded inputs. The committed fixtures let the
 oracle and the CUDA path be checked against the reference on machines where
 the reference sources are absent.
 
-Usage:  python tests/golden/make_golden.py [--reference /root/reference]
+Usage:  python tests/golden/make_golden.py [--reference PATH]
 """
 from __future__ import annotations
 
@@ -27,7 +28,8 @@ from oracle import oracle as O  # noqa: E402
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=None,
+                    help="reference checkout (default: $ENT_REFERENCE or ../reference)")
     args = ap.parse_args()
     if O.build_ref(args.reference) is None:
         raise SystemExit("reference sources not found")

@@ -2,7 +2,6 @@
 reference's own estimator sources compile and link against it unchanged
 (CPU, where the reference sources are present), and a driver calling it the
 way mi.cpp does reproduces the reference's MI output (GPU)."""
-import os
 import subprocess
 import tempfile
 from pathlib import Path
@@ -12,7 +11,9 @@ import pytest
 
 from conftest import ROOT
 
-REF = Path(os.environ.get("ENT_REFERENCE", "/root/reference"))
+from oracle import oracle as O  # noqa: E402
+
+REF = O.reference_dir() or Path("reference-sources-not-present")
 SHIM = ROOT / "entropical_gb300" / "shim"
 LIB = ROOT / "entropical_gb300" / "lib"
 
