@@ -27,7 +27,7 @@ CANDIDATES = {
     1: [(8, 2, 0), (16, 2, 0), (16, 2, 1), (16, 2, 2), (16, 2, 3), (16, 2, 4), (16, 2, 5),
         (16, 2, 6)],
     2: [(8, 2, 0), (16, 1, 2), (16, 2, 0), (16, 2, 1), (16, 2, 2), (16, 2, 3),
-        (16, 1, 4), (16, 2, 4), (16, 2, 5), (16, 4, 7), (16, 6, 7)],
+        (16, 1, 4), (16, 2, 4), (16, 2, 5), (16, 3, 7), (16, 4, 7)],
     3: [(4, 1, 0), (8, 1, 0), (8, 1, 1), (8, 1, 2), (8, 2, 2), (8, 1, 3), (8, 1, 4), (8, 2, 4),
         (8, 2, 5)],
 }

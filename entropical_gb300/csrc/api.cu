@@ -417,11 +417,15 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
       I.scale = (mode & DM_COUNT) ? 1.0 : std::pow(0.75, (double)s.d) / (s.norm * prod_hg2);
       I.out = s.out;
       if (fused[i]) {
-        // one slot per block of targets of the moment kernel, which runs its
-        // own epilogue: no tiles, no FP64 accumulator
+        // Edge tiles for the symmetric pair kernel (one run each: the strip S
+        // above); its FP64 sums go to acc. The moment kernel runs its own
+        // epilogue and writes one slot per block of targets, within tile_cap.
         I.fused = 1;
-        I.tt = moments2d_block_targets();
-        I.tile_cap = (s.n + I.tt - 1) / I.tt;
+        I.sym = 1;
+        I.tt = (uint32_t)sym_tile_targets(2, PAIR_SYM);
+        I.tile_cap = std::max((s.n + I.tt - 1) / I.tt + std::min(I.n_strips, s.n),
+                              moments2d_blocks(s.n));
+        sym_points += s.n;
       } else {
         // 2-D instances beside strip moments run the symmetric pair kernel
         const int body = (d == 2 && var_d[2] == PAIR_MOMENT) ? PAIR_SYM : var_d[d];
@@ -553,6 +557,7 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
       m.ybound = static_cast<float2*>(c.arena.alloc(8 * (size_t)hi[i].n_strips));
       m.perm = hi[i].perm;
       m.out = hi[i].out;
+      m.acc = hi[i].acc;
       m.scale = hi[i].scale;
       m.slot_base = hi[i].tile_base;
       m.P = c.arena.alloc(moments2d_prefix_bytes(hi[i].n));
@@ -668,16 +673,19 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
         r = launch_range1d(st, dr1, (uint32_t)r1.size(), r1_max_n, dr1_blk, r1_blocks, r1_tot);
         launches += 3;
       } else if (d == 2 && var_d[2] == PAIR_MOMENT) {
-        // the moments take their instances, the symmetric kernel the rest
-        r = launch_moments2d(st, dm2, (uint32_t)m2.size(), m2_max_n, m2_max_strips, dm2_blk,
-                             m2_blocks, m2_tot, c.d_logtab, tile_ls, mode);
-        launches += 4;
-        if (r == cudaSuccess && sym2) {
+        // The symmetric kernel first: the edge strips of the moment instances
+        // and every pair of the other 2-D instances. Then the moments, which
+        // add the edge sums and write the slots of their instances (the rest
+        // of those instances' slots stay zero).
+        r = cudaMemsetAsync(tile_ls + group_base[2], 0, sizeof(double) * group_slots[2], st);
+        if (r == cudaSuccess)
           r = launch_density(st, 2, c.tile_r[1], PAIR_SYM, tiles + group_base[2],
                              group_slots[2], di_sorted, wc + 2, c.d_err,
                              tile_ls + group_base[2], mode, c.n_sms, &launched);
-          launches += 1;
-        }
+        if (r == cudaSuccess)
+          r = launch_moments2d(st, dm2, (uint32_t)m2.size(), m2_max_n, m2_max_strips, dm2_blk,
+                               m2_blocks, m2_tot, c.d_logtab, tile_ls, mode);
+        launches += 5;
       } else {
         r = launch_density(st, d, c.tile_r[d - 1], var_d[d], tiles + group_base[d],
                            group_slots[d], di_sorted, wc + d, c.d_err, tile_ls + group_base[d],

@@ -62,7 +62,7 @@ struct Ctx {
   // and it is faster on small supports). An explicit choice (set_tuning, the
   // autotuner) clears it: then every 2-D instance takes the moments.
   bool moment_auto = true;
-  uint32_t moment_cells = 4;  // strips per bandwidth of PAIR_MOMENT (2..12)
+  uint32_t moment_cells = 3;  // strips per bandwidth of PAIR_MOMENT (2..12)
   bool use_graphs = true;       // capture the batch kernel sequence in a CUDA graph
 
   // grid of a persistent kernel: resident CTAs per SM x SMs, capped by work

@@ -317,7 +317,7 @@ std::vector<TuneCand> tune_candidates(uint32_t d) {
   if (d == 1) return {{2, 16, 2}, {4, 16, 2}, {5, 16, 2}, {PAIR_RANGE, 16, 2}};
   if (d == 2)
     return {{2, 16, 2},           {4, 16, 1},           {4, 16, 2},          {4, 16, 3},
-            {5, 16, 2},           {PAIR_MOMENT, 16, 4}, {PAIR_MOMENT, 16, 6}};
+            {5, 16, 2},           {PAIR_MOMENT, 16, 3}, {PAIR_MOMENT, 16, 4}};
   return {{1, 8, 1}, {2, 8, 1}, {4, 8, 1}, {4, 8, 2}, {5, 8, 1}};
 }
 

@@ -253,7 +253,7 @@ __global__ void k_plan(const InstDev* __restrict__ insts, uint32_t n_inst,
   const uint32_t t = (g - I.tile_base) / parts;
   td.part = (g - I.tile_base) % parts;
   const uint32_t total = I.tile_off[I.n_strips];
-  if (t >= total || I.fused) {  // strip-moment instances have no tiles
+  if (t >= total) {
     tiles[g] = td;
     return;
   }
@@ -301,8 +301,15 @@ __global__ void k_plan(const InstDev* __restrict__ insts, uint32_t n_inst,
   } else if (d == 2) {
     const int S = (int)I.S;
     const int c1 = (int)s;
-    for (int c = max(0, c1 - S); c <= min((int)I.ncell1 - 1, c1 + S); ++c)
-      add_strip((uint32_t)c);
+    if (I.fused) {
+      // strip moments: the tile's only run is the strip S above it, where
+      // the y edge of its targets' support falls (the one S below is the run
+      // of that strip's own tiles, so each edge pair is evaluated once)
+      if (c1 + S < (int)I.ncell1) add_strip((uint32_t)(c1 + S));
+    } else {
+      for (int c = max(0, c1 - S); c <= min((int)I.ncell1 - 1, c1 + S); ++c)
+        add_strip((uint32_t)c);
+    }
   } else {
     const int S = (int)I.S, S2 = (int)I.S2;
     const int c1 = (int)(s / I.ncell2), c2 = (int)(s % I.ncell2);

@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(NW * 32, MINB)
         const TileDesc* T = tiles + g;
         const uint32_t nr = T->n_runs;
         s_tb = T->t_begin;
-        s_tc = insts[T->inst].fused ? 0u : T->t_count;  // moment-owned: skip
+        s_tc = T->t_count;
         s_inst = T->inst;
         s_nr = nr;
         run_pre[0] = 0;

@@ -71,8 +71,10 @@ struct InstDev {
   uint32_t parts;           // work items per tile (source runs split; 0 = 1);
                             // tile_cap counts work-item slots
   double* acc;              // symmetric mode: unscaled sums by sorted position
-  uint32_t fused;           // 1: the strip-moment kernel owns this instance
-                            // (no tiles; pair kernel and finish skip it)
+  uint32_t fused;           // 1: the strip-moment kernel owns this instance:
+                            // its tiles carry only the edge run (the strip S
+                            // above), the symmetric pair kernel sums those
+                            // pairs into acc and its finish skips it
   uint32_t pad2;
 };
 
@@ -148,9 +150,10 @@ __host__ __device__ constexpr bool pair_is_sym(int v) {
 // and is finished by launch_sym_finish like the symmetric bodies.
 constexpr int PAIR_RANGE = 6;
 // Pair body PAIR_MOMENT (d = 2 only, moments2d.cu): per target and strip,
-// the x-support is one index range; strips wholly inside the y-support are
-// summed from exact fixed-point moment prefix sums, the others pair by pair.
-// Writes InstDev::acc like PAIR_RANGE.
+// the x-support is one index range; strips within S - 1 of the target's own
+// are summed from exact fixed-point moment prefix sums, the two edge strips
+// at distance S pair by pair by the symmetric kernel (edge-only tiles), which
+// runs first and leaves its sums in InstDev::acc.
 constexpr int PAIR_MOMENT = 7;
 constexpr uint64_t MOMENT_MIN_POINTS = 1000000;  // default rule: see Ctx::moment_auto
 // Default rule per instance: the moments take a 2-D instance with at least
@@ -188,8 +191,10 @@ struct Mom2D {
   void* P;                      // (n + 1) x 8 moment prefix sums, 128-bit each
   const uint32_t* perm;         // original index of every sorted position
   double* out;                  // per-point density by original index (nullable)
+  const double* acc;            // edge-strip sums by sorted position (InstDev::acc)
   double scale;                 // InstDev::scale
-  uint32_t n, n_strips, S;      // S: strips examined on each side
+  uint32_t n, n_strips, S;      // strips within S - 1 of a target's own are
+                                // summed here, those at S by the pair kernel
   float g2[2];
   uint32_t chunk_base;          // first prefix chunk of the instance
   uint32_t blk_base;            // first target block of the instance

@@ -20,14 +20,17 @@
 //    map and the true value lies in (-2^124, 2^124), so the signed modular
 //    result IS the exact integer: no cancellation whatever the offset or
 //    spread of the data;
-//  * otherwise (the strip crosses the edge of the y-support, at most two
-//    strips per target) the pairs of [l, r) are evaluated one by one.
+//  * the strips at distance exactly S from the target's own (where the edge
+//    of its y-support falls) are summed pair by pair by the symmetric pair
+//    kernel, each pair once for both points (the plan gives every strip one
+//    tile run: the strip S above it); strips nearer than S whose y extent
+//    still crosses the support (rounding at the widened cell edges) are
+//    summed pair by pair here.
 // Fixed-point rounding of the coordinates (2^-23 g) changes a kernel value
 // by less than 2^-21 g^2 per dimension, far below the 1e-5 density bar.
 //
 // The epilogue (scale, per-point output, FP64 log and per-block sums) runs
-// in the same kernel; the tile plan leaves these instances without tiles and
-// the pair kernel and its finish skip them.
+// in the same kernel; the symmetric kernel's finish skips these instances.
 #include <algorithm>
 
 #include "engine.h"
@@ -65,7 +68,51 @@ __device__ __forceinline__ u128 quant(float v) {
   return (b & 0x80000000u) ? (u128)0 - q : q;
 }
 
+// quant<23> of a value below 2^8 in magnitude (|result| < 2^31), with the
+// same rounding (half away from zero).
+__device__ __forceinline__ int32_t quant23_narrow(float v) {
+  const uint32_t b = __float_as_uint(v);
+  const int e = (int)((b >> 23) & 0xffu);
+  const uint32_t m = (b & 0x7fffffu) | 0x800000u;
+  const int sh = e - 127;  // <= 7
+  uint32_t q;
+  if (e == 0) q = 0;
+  else if (sh >= 0) q = m << sh;
+  else if (sh > -25) q = (m + (1u << (-sh - 1))) >> (-sh);
+  else q = 0;
+  return (b & 0x80000000u) ? -(int32_t)q : (int32_t)q;
+}
+
+// both coordinates below 2^8 in magnitude (scaled units)
+__device__ __forceinline__ bool narrow2(float2 p) {
+  return ((__float_as_uint(p.x) >> 23) & 0xffu) < 135u &&
+         ((__float_as_uint(p.y) >> 23) & 0xffu) < 135u;
+}
+
+__device__ __forceinline__ u128 u128_of(int64_t hi, uint64_t lo) {
+  return ((u128)(uint64_t)hi << 64) | lo;
+}
+
+// The eight moments of one point modulo 2^128. Points whose scaled
+// coordinates lie below 2^8 in magnitude (all of them for data within a few
+// hundred bandwidths of zero) take 32-bit coordinates and 64 x 64 -> 128-bit
+// products; the others the general 128-bit form. Both give the same residues.
 __device__ __forceinline__ void moments(float2 p, u128 (&m)[NM]) {
+  if (narrow2(p)) {
+    const int32_t x = quant23_narrow(p.x), y = quant23_narrow(p.y);
+    const int64_t X2 = (int64_t)x * x, Y2 = (int64_t)y * y, XY = (int64_t)x * y;
+    const int64_t X = x, Y = y;
+    m[0] = (u128)(__int128)x;
+    m[1] = (u128)(__int128)y;
+    m[2] = (u128)(uint64_t)X2;
+    m[3] = (u128)(__int128)XY;
+    m[4] = (u128)(uint64_t)Y2;
+    m[5] = u128_of(__mul64hi(X2, Y), (uint64_t)X2 * (uint64_t)Y);
+    m[6] = u128_of(__mul64hi(X, Y2), (uint64_t)X * (uint64_t)Y2);
+    m[7] = u128_of((int64_t)__umul64hi((uint64_t)X2, (uint64_t)Y2),
+                   (uint64_t)X2 * (uint64_t)Y2);
+    return;
+  }
   const u128 X = quant<23>(p.x), Y = quant<23>(p.y);
   const u128 X2 = X * X, Y2 = Y * Y;
   m[0] = X;
@@ -76,6 +123,28 @@ __device__ __forceinline__ void moments(float2 p, u128 (&m)[NM]) {
   m[5] = X2 * Y;
   m[6] = X * Y2;
   m[7] = X2 * Y2;
+}
+
+// The M2_E points of one prefix thread, loaded at once (16-byte loads when
+// all are present: pts is 256-byte aligned and k0 a multiple of 8); returns
+// how many are present.
+__device__ __forceinline__ uint32_t load_points8(const float2* __restrict__ pts, uint64_t k0,
+                                                 uint32_t n, float2 (&p)[M2_E]) {
+  static_assert(M2_E == 8, "four 16-byte loads per thread");
+  if (k0 + M2_E <= n) {
+    const float4* q = reinterpret_cast<const float4*>(pts + k0);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const float4 v = q[i];
+      p[2 * i] = make_float2(v.x, v.y);
+      p[2 * i + 1] = make_float2(v.z, v.w);
+    }
+    return M2_E;
+  }
+  const uint32_t ne = k0 < n ? (uint32_t)(n - k0) : 0u;
+#pragma unroll
+  for (uint32_t e = 0; e < M2_E; ++e) p[e] = e < ne ? pts[k0 + e] : make_float2(0.f, 0.f);
+  return ne;
 }
 
 __device__ __forceinline__ u128 shfl_up128(u128 v, int o) {
@@ -152,13 +221,16 @@ __global__ void __launch_bounds__(M2_PT)
   const uint64_t b0 = (uint64_t)blockIdx.x * M2_CHUNK;
   if (b0 >= M.n) return;  // block-uniform
   const uint64_t k0 = b0 + (uint64_t)threadIdx.x * M2_E;
+  float2 pt[M2_E];
+  const uint32_t ne = load_points8(M.pts, k0, M.n, pt);
   u128 s[NM];
 #pragma unroll
   for (int m = 0; m < NM; ++m) s[m] = 0;
+#pragma unroll
   for (uint32_t e = 0; e < M2_E; ++e)
-    if (k0 + e < M.n) {
+    if (e < ne) {
       u128 q[NM];
-      moments(M.pts[k0 + e], q);
+      moments(pt[e], q);
 #pragma unroll
       for (int m = 0; m < NM; ++m) s[m] += q[m];
     }
@@ -255,107 +327,161 @@ __device__ __forceinline__ float pair_term(float2 p, float2 t, float g1, float g
   return __fmaf_rn(__fmaf_rn(-dx, dx, g1), wy, acc);
 }
 
-// Unscaled density sum of sorted position k of instance M (see the top).
-__device__ __forceinline__ double target_sum(const Mom2D& M, uint32_t k) {
-  const float2* __restrict__ pts = M.pts;
-  const uint32_t* __restrict__ ss = M.strip_start;
-  const u128* __restrict__ P = static_cast<const u128*>(M.P);
-  const float2 t = pts[k];
-  const float g1 = M.g2[0], g2 = M.g2[1];
-  const uint32_t s = M.skeys[k];
-  const uint32_t s_lo = s >= M.S ? s - M.S : 0u;
-  const uint32_t s_hi = min(M.n_strips - 1, s + M.S);
-  const u128 TX = quant<23>(t.x), TY = quant<23>(t.y);
-  const u128 c0 = quant<46>(g1) - TX * TX, c1 = TX + TX;
-  const u128 d0 = quant<46>(g2) - TY * TY, d1 = TY + TY;
-  u128 ex = 0;
-  double fs = 0.0;
-  for (uint32_t sp = s_lo; sp <= s_hi; ++sp) {
-    const uint32_t a = ss[sp], b = ss[sp + 1];
-    if (a == b) continue;
-    const float2 yb = M.ybound[sp];
-    const bool in_lo = insup(yb.x, t.y, g2), in_hi = insup(yb.y, t.y, g2);
-    if ((!in_lo && yb.x >= t.y) || (!in_hi && yb.y <= t.y)) continue;  // all out
-    // x-support range [l, r) of the strip
-    uint32_t l = a, r = b;
-    while (l < r) {
-      const uint32_t m = l + ((r - l) >> 1);
-      const float xm = pts[m].x;
-      if (xm < t.x && !insup(xm, t.x, g1)) l = m + 1; else r = m;
-    }
-    r = b;
-    uint32_t e = l;
-    while (e < r) {
-      const uint32_t m = e + ((r - e) >> 1);
-      const float xm = pts[m].x;
-      if (xm > t.x && !insup(xm, t.x, g1)) r = m; else e = m + 1;
-    }
-    r = e;
-    if (l >= r) continue;
-    if (in_lo && in_hi) {
-      const u128* pl = P + NM * (size_t)l;
-      const u128* pr = P + NM * (size_t)r;
-      u128 mo[NM];
-#pragma unroll
-      for (int m = 0; m < NM; ++m) mo[m] = pr[m] - pl[m];
-      const u128 cnt = (u128)(r - l);
-      // sum_b d_b M_ab for a = 0, 1, 2 (d_2 = -1), then sum_a c_a (.) (c_2 = -1)
-      const u128 e0 = d0 * cnt + d1 * mo[1] - mo[4];
-      const u128 e1 = d0 * mo[0] + d1 * mo[3] - mo[6];
-      const u128 e2 = d0 * mo[2] + d1 * mo[5] - mo[7];
-      ex += c0 * e0 + c1 * e1 - e2;
-    } else {
-      // four independent chains keep four loads in flight
-      float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
-      uint32_t j = l;
-      for (; j + 4 <= r; j += 4) {
-        const float2 p0 = pts[j], p1 = pts[j + 1], p2 = pts[j + 2], p3 = pts[j + 3];
-        a0 = pair_term(p0, t, g1, g2, a0);
-        a1 = pair_term(p1, t, g1, g2, a1);
-        a2 = pair_term(p2, t, g1, g2, a2);
-        a3 = pair_term(p3, t, g1, g2, a3);
-      }
-      for (; j < r; ++j) a0 = pair_term(pts[j], t, g1, g2, a0);
-      fs += (double)((a0 + a1) + (a2 + a3));
-    }
+// x-support of a target at tx in the x-sorted points of one strip, searched
+// in [lo, hi) with the pair kernels' own test (monotone in the position and
+// in tx): the first position not left of the support, and the first one
+// right of it.
+__device__ __forceinline__ uint32_t first_not_left(const float2* __restrict__ pts, uint32_t lo,
+                                                   uint32_t hi, float tx, float g1) {
+  while (lo < hi) {
+    const uint32_t m = lo + ((hi - lo) >> 1);
+    const float xm = pts[m].x;
+    if (xm < tx && !insup(xm, tx, g1)) lo = m + 1; else hi = m;
   }
-  // 2^-92 converts the fixed-point products back to units of g^4
-  return s128_to_double(ex) * 0x1p-92 + fs;
+  return lo;
+}
+__device__ __forceinline__ uint32_t first_right(const float2* __restrict__ pts, uint32_t lo,
+                                                uint32_t hi, float tx, float g1) {
+  while (lo < hi) {
+    const uint32_t m = lo + ((hi - lo) >> 1);
+    const float xm = pts[m].x;
+    if (xm > tx && !insup(xm, tx, g1)) hi = m; else lo = m + 1;
+  }
+  return lo;
 }
 
-// One thread per target, with the epilogue of the other bodies' finish
-// kernel fused: density = scale x sum, written by original index and/or
-// logged (FP64) and summed per block of targets in a fixed order; the
-// block sums land in the instance's slots of tile_logsum.
+constexpr int M2_MAX_IN = 23;  // inside strips per target: 2S - 1, S <= 12
+
+// One thread per target; a warp holds 32 consecutive sorted positions. The
+// strips within S - 1 of the target's own strip are inside its y-support
+// (checked per strip against the strip's y extent); the two strips at
+// distance S, where the support's y edge falls, are summed pair by pair by
+// the symmetric pair kernel beforehand (its FP64 sums arrive in M.acc).
+//
+// Searches. When the warp's 32 targets lie in one strip they are x-sorted,
+// and the support bounds in any other strip are monotone in the target's x.
+// The warp first finds, for every inside strip at once (one bisection per
+// lane), the bounds of its first and last target; each lane then searches
+// only between them -- a range of about as many points as the warp's x-span
+// holds, instead of the whole strip. Other warps (strip boundaries, the end
+// of an instance) search each strip in full.
+//
+// Sums. The moment rows of all inside strips are added first (128-bit, in
+// registers) and combined with the target's coefficients once; strips whose
+// y extent crosses the support (rounding at the widened cell edges only)
+// are summed pair by pair.
+//
+// Epilogue as the other bodies' finish kernel: density = scale x sum,
+// written by original index and/or logged (FP64) and summed per block of
+// targets in a fixed order into the instance's slots of tile_logsum.
 __global__ void __launch_bounds__(M2_TB, 10)
     k_m2_density(const Mom2D* __restrict__ ms, uint32_t n_inst,
                  const uint32_t* __restrict__ blk_base, const double2* __restrict__ logtab,
                  double* __restrict__ tile_logsum, uint32_t mode) {
   __shared__ double s_part[M2_TB / 32];
-  const uint32_t g = blockIdx.x;
+  __shared__ uint32_t s_br[M2_TB / 32][4 * M2_MAX_IN];
+  const uint32_t gb = blockIdx.x;
   uint32_t lo = 0, hi = n_inst;
   while (hi - lo > 1) {
     const uint32_t m = (lo + hi) / 2;
-    if (blk_base[m] <= g) lo = m; else hi = m;
+    if (blk_base[m] <= gb) lo = m; else hi = m;
   }
   const Mom2D& M = ms[lo];
-  const uint32_t blk = g - M.blk_base;
+  const uint32_t blk = gb - M.blk_base;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t k = blk * M2_TB + threadIdx.x;
+  const bool valid = k < M.n;
+  const float2* __restrict__ pts = M.pts;
+  const uint32_t* __restrict__ ss = M.strip_start;
+  const u128* __restrict__ P = static_cast<const u128*>(M.P);
+  const float g1 = M.g2[0], g2 = M.g2[1];
+  const int S = (int)M.S, n_strips = (int)M.n_strips;
+  const float2 t = pts[valid ? k : M.n - 1];
+  const int s = (int)M.skeys[valid ? k : M.n - 1];
+  const int s0 = __shfl_sync(FULL_MASK, s, 0);
+  const bool uni = __all_sync(FULL_MASK, valid && s == s0);
+  if (uni) {
+    // bounds of the warp's first and last target in every inside strip
+    const float tmin = __shfl_sync(FULL_MASK, t.x, 0), tmax = __shfl_sync(FULL_MASK, t.x, 31);
+    for (int q = lane; q < 4 * (2 * S - 1); q += 32) {
+      const int sp = s0 + q / 4 - (S - 1);
+      uint32_t res = 0;
+      if (sp >= 0 && sp < n_strips) {
+        const uint32_t a = ss[sp], b = ss[sp + 1];
+        const float tq = (q & 1) ? tmax : tmin;
+        res = (q & 2) ? first_right(pts, a, b, tq, g1) : first_not_left(pts, a, b, tq, g1);
+      }
+      s_br[warp][q] = res;
+    }
+    __syncwarp();
+  }
+  u128 mo[NM];
+#pragma unroll
+  for (int m = 0; m < NM; ++m) mo[m] = 0;
+  uint32_t cnt = 0;
+  float fs = 0.f;
+  for (int o = -(S - 1); o <= S - 1; ++o) {
+    const int sp = s + o;
+    if (sp < 0 || sp >= n_strips) continue;
+    const uint32_t a = ss[sp], b = ss[sp + 1];
+    if (a == b) continue;
+    const float2 yb = M.ybound[sp];
+    const bool in_lo = insup(yb.x, t.y, g2), in_hi = insup(yb.y, t.y, g2);
+    if ((!in_lo && yb.x >= t.y) || (!in_hi && yb.y <= t.y)) continue;  // all out
+    uint32_t llo = a, lhi = b, rlo = a, rhi = b;
+    if (uni) {
+      const uint32_t* br = s_br[warp] + 4 * (o + S - 1);
+      llo = br[0];
+      lhi = br[1];
+      rlo = br[2];
+      rhi = br[3];
+    }
+    const uint32_t l = first_not_left(pts, llo, lhi, t.x, g1);
+    const uint32_t r = first_right(pts, max(rlo, l), rhi, t.x, g1);
+    if (l >= r) continue;
+    if (in_lo && in_hi) {
+      const u128* pl = P + NM * (size_t)l;
+      const u128* pr = P + NM * (size_t)r;
+#pragma unroll
+      for (int m = 0; m < NM; ++m) mo[m] += pr[m] - pl[m];
+      cnt += r - l;
+    } else {
+      float a0 = 0.f, a1 = 0.f;
+      uint32_t j = l;
+      for (; j + 2 <= r; j += 2) {
+        a0 = pair_term(pts[j], t, g1, g2, a0);
+        a1 = pair_term(pts[j + 1], t, g1, g2, a1);
+      }
+      if (j < r) a0 = pair_term(pts[j], t, g1, g2, a0);
+      fs += a0 + a1;
+    }
+  }
   double v = 0.0;  // this target's term of the block sum
-  if (k < M.n) {
-    const double dens = M.scale * target_sum(M, k);
+  if (valid) {
+    // sum_b d_b M_ab for a = 0, 1, 2 (d_2 = -1), then sum_a c_a (.) (c_2 = -1)
+    const u128 TX = quant<23>(t.x), TY = quant<23>(t.y);
+    const u128 c0 = quant<46>(g1) - TX * TX, c1 = TX + TX;
+    const u128 d0 = quant<46>(g2) - TY * TY, d1 = TY + TY;
+    const u128 e0 = d0 * (u128)cnt + d1 * mo[1] - mo[4];
+    const u128 e1 = d0 * mo[0] + d1 * mo[3] - mo[6];
+    const u128 e2 = d0 * mo[2] + d1 * mo[5] - mo[7];
+    const u128 ex = c0 * e0 + c1 * e1 - e2;
+    // 2^-92 converts the fixed-point products back to units of g^4
+    double sum = s128_to_double(ex) * 0x1p-92 + (double)fs;
+    if (M.acc) sum += M.acc[k];
+    const double dens = M.scale * sum;
     if (mode & DM_WRITE_F64) M.out[M.perm[k]] = dens;
     if (mode & DM_LOGSUM) v = log_fp64(dens, logtab);
     else if (mode & DM_SUMV) v = dens;
   }
   if (mode & (DM_LOGSUM | DM_SUMV)) {  // block-uniform
     for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(FULL_MASK, v, o);
-    if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = v;
+    if (lane == 0) s_part[warp] = v;
     __syncthreads();
     if (threadIdx.x == 0) {
-      double t = 0.0;
-      for (uint32_t w = 0; w < M2_TB / 32; ++w) t += s_part[w];
-      tile_logsum[M.slot_base + blk] = t;
+      double tsum = 0.0;
+      for (uint32_t w = 0; w < M2_TB / 32; ++w) tsum += s_part[w];
+      tile_logsum[M.slot_base + blk] = tsum;
     }
   }
 }
