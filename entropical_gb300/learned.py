@@ -18,6 +18,7 @@ from __future__ import annotations
 
 import argparse
 import ctypes as C
+import json
 import time
 from pathlib import Path
 
@@ -245,6 +246,79 @@ def train(ctx: Context, X, T, M, epochs: int = 30, batch: int = 256, lr: float =
     return net, losses
 
 
+# The reference's AMISE objective (hestimate.cpp:41-53) falls monotonically
+# in h on continuous data, so its bracket search (hestimate.cpp:55-86)
+# keeps the upper half at every level and returns h0 (2 - 1.9/512) for every
+# column. The trained network can only learn this constant; the constant arm
+# below is the baseline it is judged against.
+CONSTANT_RATIO = 2.0 - 1.9 / 512.0
+
+
+def generate(n_mix: int, seed: int, n_min: int = 5_000, n_max: int = 200_000):
+    """n_mix generated mixtures (d in 1..3, N log-uniform in [n_min, n_max])."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n_mix):
+        d = int(rng.integers(1, 4))
+        n = int(np.exp(rng.uniform(np.log(n_min), np.log(n_max))))
+        out.append(mixture_instance(rng, d, n))
+    return out
+
+
+def hestimate_constant(ctx: Context, items, ratio: float = CONSTANT_RATIO,
+                       skip_levels: int = 6):
+    """The warm-started search entered at h0 * ratio for every dimension (no
+    network): per instance, the rule of thumb, then the warm search. Returns
+    (h (n, 3), stats) like hestimate_learned."""
+    from .densities import HEST_AMISE_WARM, HEST_THUMB
+    h = np.zeros((len(items), 3), np.float32)
+    stats = []
+    for q, x in enumerate(items):
+        x = np.atleast_2d(x)
+        h0, _ = ctx.hestimate(x, HEST_THUMB)
+        hq, st = ctx.hestimate(x, HEST_AMISE_WARM, h_init=h0 * np.float32(ratio),
+                               skip_levels=skip_levels)
+        h[q, :len(hq)] = hq
+        stats.append(st + [dict(h0=0.0, conv_evals=0, levels_skipped=0, warm_converged=1)] *
+                     (3 - len(hq)))
+    return h, stats
+
+
+def evaluate(ctx: Context, net: BandwidthMLP, items, skip_levels: int = 6) -> dict:
+    """Held-out evaluation of the warm start, three arms: the full search
+    (no warm start), the network's warm start and the constant-offset warm
+    start. Per arm: convolution passes, fallbacks to the full search, the
+    largest bandwidth difference to the full search, and the largest entropy
+    difference (library entropies at each arm's bandwidths against those at
+    the full search's). Returns a dict; the per-instance bandwidths of the
+    full search are in "h_full"."""
+    dims = [np.atleast_2d(x).shape[0] for x in items]
+    h_full, st_full = hestimate_full(ctx, items)
+    h_net, st_net = hestimate_learned(ctx, net, items, skip_levels=skip_levels)
+    h_con, st_con = hestimate_constant(ctx, items, skip_levels=skip_levels)
+
+    def entropies(h):
+        return ctx.entropy_batch([(x, h[q, :dims[q]]) for q, x in enumerate(items)])
+
+    H_full = entropies(h_full)
+    cols = int(sum(dims))
+    out = {"instances": len(items), "columns": cols, "skip_levels": int(skip_levels),
+           "h_full": h_full, "H_full": H_full}
+    for name, h, st in (("none", h_full, st_full), ("network", h_net, st_net),
+                        ("constant", h_con, st_con)):
+        evals = sum(st[q][j]["conv_evals"] for q in range(len(items)) for j in range(dims[q]))
+        fall = sum(1 - st[q][j]["warm_converged"] for q in range(len(items))
+                   for j in range(dims[q])) if name != "none" else 0
+        dh = max(float(np.max(np.abs(h[q, :dims[q]] - h_full[q, :dims[q]]) / h_full[q, :dims[q]]))
+                 for q in range(len(items)))
+        H = H_full if name == "none" else entropies(h)
+        out[name] = {"conv_evals": int(evals), "conv_evals_per_column": evals / cols,
+                     "fallbacks": int(fall), "max_rel_dh_vs_full": dh,
+                     "max_abs_dH_vs_full": float(np.max(np.abs(H - H_full))),
+                     "identical_h": bool(np.array_equal(h[:, :], h_full[:, :]))}
+    return out
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description="train the bandwidth warm-start network")
     ap.add_argument("--n-mix", type=int, default=20_000)
@@ -264,11 +338,17 @@ def main(argv=None):
         X, T, M = make_dataset(ctx, args.n_mix, args.seed, log=print)
         if args.dataset:
             np.savez_compressed(args.dataset, X=X, T=T, M=M)
-    print("labels r: mean", float(T[M > 0].mean()), "sd", float(T[M > 0].std()))
+    print("labels r: mean", float(T[M > 0].mean()), "sd", float(T[M > 0].std()),
+          "constant log ratio", float(np.log(CONSTANT_RATIO)))
     net, losses = train(ctx, X, T, M, epochs=args.epochs, lr=args.lr, log=print)
     Path(args.out).parent.mkdir(parents=True, exist_ok=True)
     net.save(args.out)
     print("saved", args.out, "final loss", losses[-1])
+    if args.n_held > 0:
+        # held-out mixtures from the same generator with another seed
+        ev = evaluate(ctx, net, generate(args.n_held, args.seed + 1000))
+        ev = {k: v for k, v in ev.items() if k not in ("h_full", "H_full")}
+        print("held-out", json.dumps(ev))
 
 
 if __name__ == "__main__":

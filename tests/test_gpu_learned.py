@@ -56,6 +56,34 @@ def test_training_and_warm_start_gain(ctx):
     evals_warm = sum(s["conv_evals"] for row in st_warm for s in row)
     # 16 convolutions per column without the network, 4 with it
     assert evals_warm * 4 == evals_full
+    # The constant-offset warm start (no network) does exactly as well: the
+    # reference's AMISE objective falls monotonically in h, so every label is
+    # the same ratio and the network has nothing else to learn.
+    h_const, st_const = learned.hestimate_constant(ctx, held, skip_levels=6)
+    assert np.array_equal(h_full, h_const)
+    evals_const = sum(s["conv_evals"] for row in st_const for s in row)
+    assert evals_const == evals_warm
+    assert np.allclose(T[M > 0], np.log(learned.CONSTANT_RATIO), atol=1e-6)
     # the bandwidth search agrees with the restated reference search
     x0 = held[0][0]
     assert O.hestimate_amise(x0)[0] == h_full[0, 0]
+
+
+def test_held_out_evaluation_against_fp64(ctx):
+    """The committed network on held-out mixtures: the three arms (full
+    search, network, constant offset) give the same bandwidths, the warm
+    starts never fall back, and the entropies at those bandwidths agree with
+    the FP64 oracle's entropy at the full search's bandwidths."""
+    net = learned.BandwidthMLP.load(ctx)
+    held = learned.generate(24, seed=4242, n_min=3000, n_max=20000)
+    ev = learned.evaluate(ctx, net, held)
+    cols = ev["columns"]
+    assert ev["none"]["conv_evals"] == 16 * cols
+    for arm in ("network", "constant"):
+        assert ev[arm]["identical_h"] and ev[arm]["fallbacks"] == 0
+        assert ev[arm]["conv_evals"] == 4 * cols
+        assert ev[arm]["max_abs_dH_vs_full"] == 0.0
+    for q, x in enumerate(held):
+        d = x.shape[0]
+        ref = O.entropy_fp64(x, ev["h_full"][q, :d])
+        assert abs(ev["H_full"][q] - ref) < 1e-6, (q, ev["H_full"][q], ref)
