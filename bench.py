@@ -64,6 +64,10 @@ def parse():
                     help="keep the library's default tile shapes (no autotuner pass)")
     ap.add_argument("--cells-per-h3", type=int, default=0,
                     help="cells per bandwidth of 3-D strips (1 or 2; default: the library's)")
+    ap.add_argument("--te-coords", type=int, default=0,
+                    help="time only the transfer-entropy batch over the first N coordinates of "
+                         "the 32 x 200k Langevin data (lags 1, 5, 10): the small case for ncu "
+                         "captures of the 3-D kernel; prints a JSON line of its own")
     ap.add_argument("--coords", type=int, default=N_COORDS,
                     help="coordinates of the MI batch (64 = the benchmark workload; "
                          "smaller values give the small case used for ncu captures)")
@@ -185,6 +189,21 @@ def moment_roofline(t2: float, points_2d: int) -> dict:
             "peak_kind": note,
             "issue_frac_ncu": profile_figure(prof, "issue_frac"),
             "note": "load-latency bound gather; see issue_frac_ncu and the profile"}
+
+
+def roofline_3d(pairs: float, ms: float) -> dict:
+    """The 3-D symmetric pair kernel against the FP32 CUDA-core peak: 14
+    flops per evaluated unordered pair (its body), with the FMA-pipe busy
+    fraction of the committed ncu summary."""
+    import torch
+    peak, note = fp32_peak_tflops(torch.cuda.get_device_properties(0).multi_processor_count)
+    prof = "density3d_sym_te4_ncu.md"
+    fpp = profile_figure(prof, "flops_per_pair") or 14.0
+    achieved = fpp * pairs / (ms / 1e3) / 1e12
+    return {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak, "kernel": "k_density_sym<3,16,5,4>", "flops_per_pair": fpp,
+            "ordered_equivalent_tflops": 30.0 * pairs / (ms / 1e3) / 1e12,
+            "fma_pipe_frac_ncu": profile_figure(prof, "fma_pipe_frac"), "peak_kind": note}
 
 
 def ncu_traffic() -> float | None:
@@ -468,6 +487,7 @@ def other_configs(ctx):
         "support_pairs_3d": sup3, "candidate_pairs_3d": st.candidate_pairs_by_dim[2],
         "h2d_bytes": int(xt.nbytes),
         "max_abs_err_vs_fp64": te_err, "fp64_oracle_entries": 4, "fp64_oracle_s": t_fp64,
+        "roofline_3d": roofline_3d(st.candidate_pairs_by_dim[2], st.pair_kernel_ms_by_dim[2]),
         "cpu_baseline": {"s": t_cpu3, "pairs_per_s": sup_s3 / t_cpu3,
                          "sample": "3-D density (x5[t+5], x5[t], x17[t]) at 200k frames",
                          "extrapolated_3d_s": sup3 / (sup_s3 / t_cpu3), "kind": "port"}}
@@ -618,8 +638,36 @@ def reference_arm(args, x, h):
     print(json.dumps(line), flush=True)
 
 
+def te_only(args):
+    """Transfer entropy of all ordered pairs of the first --te-coords
+    Langevin coordinates (200k frames, lags 1, 5, 10), device time per call."""
+    import torch
+    from entropical_gb300 import Context, workloads
+    xt, _ = workloads.langevin(32, 200_000, seed=11)
+    x = np.ascontiguousarray(xt[:args.te_coords])
+    h = workloads.scott_bandwidth(xt, 3)[:args.te_coords]
+    ctx = Context(0)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    for _ in range(args.warmup):
+        ctx.te_all_pairs(x, h, [1, 5, 10])
+    ms, by_dim = [], []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        ctx.te_all_pairs(x, h, [1, 5, 10])
+        st = ctx.last_stats()
+        ms.append(st.total_ms)
+        by_dim.append(list(st.pair_kernel_ms_by_dim))
+    print(json.dumps({"workload": f"TE, {x.shape[0]} coords x 200k, lags 1, 5, 10",
+                      "ms": statistics.mean(ms), "pair_kernel_ms_by_dim": by_dim[-1],
+                      "candidate_pairs_by_dim": list(ctx.last_stats().candidate_pairs_by_dim)}),
+          flush=True)
+
+
 def main():
     args = parse()
+    if args.te_coords:
+        return te_only(args)
     ws, rank, local = dist_env()
     from entropical_gb300 import workloads
     # weak scaling over independent problems: rank r computes the benchmark
