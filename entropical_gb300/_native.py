@@ -73,6 +73,12 @@ SIGNATURES: dict[str, tuple] = {
     "ent_mi_all_pairs_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t,
                                           c_f32_p, C.c_uint32, c_f64_p, c_f64_p]),
     "ent_entropy_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_uint32, c_f64_p]),
+    "ent_mi_entropies_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, c_f32_p,
+                                          C.POINTER(C.c_uint64), C.c_size_t, C.c_uint32,
+                                          c_f64_p]),
+    "ent_te_entropies_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, c_f32_p,
+                                          c_u32_p, C.c_size_t, C.POINTER(C.c_uint64), C.c_size_t,
+                                          C.c_uint32, c_f64_p]),
     "ent_reference_estimator": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t,
                                           c_f32_p, C.c_uint32, C.c_uint32, C.c_uint32,
                                           c_f64_p]),

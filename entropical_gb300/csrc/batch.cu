@@ -54,6 +54,110 @@ int run_entropies(Ctx& c, const std::vector<ViewSpec>& views,
   return ENT_OK;
 }
 
+// The densities of an all-pairs MI in batch order: the n_cols 1-D
+// marginals, then the joints (i, j), i < j, in row order.
+void mi_build(const Ctx& c, const float* dc, size_t n_rows, size_t n_cols, const float* h,
+              std::vector<ViewSpec>* views, std::vector<InstSpec>* insts) {
+  views->resize(n_cols);
+  for (size_t j = 0; j < n_cols; ++j) (*views)[j] = {dc + j * n_rows, (uint32_t)n_rows};
+  insts->reserve(n_cols + n_cols * (n_cols - 1) / 2);
+  for (size_t i = 0; i < n_cols; ++i) {
+    InstSpec I;
+    I.d = 1;
+    I.n = (uint32_t)n_rows;
+    I.view[0] = (uint32_t)i;
+    I.h[0] = h[i];
+    I.norm = (double)n_rows;
+    I.S = c.strip_subdiv;
+    insts->push_back(I);
+  }
+  for (size_t i = 0; i < n_cols; ++i)
+    for (size_t j = i + 1; j < n_cols; ++j) {
+      InstSpec I;
+      I.d = 2;
+      I.n = (uint32_t)n_rows;
+      I.view[0] = (uint32_t)i;
+      I.view[1] = (uint32_t)j;
+      I.h[0] = h[i];
+      I.h[1] = h[j];
+      I.norm = (double)n_rows;
+      I.S = c.strip_subdiv;
+      insts->push_back(I);
+    }
+}
+
+// The densities of an all-ordered-pairs TE over the lags in batch order:
+// per lag [M 1-D y][M 2-D (y+, y)][M(M-1)/2 2-D (y_i, x_j), i < j]
+// [M(M-1) 3-D (y+, y, x)].
+void te_build(const Ctx& c, const float* dc, size_t n_rows, size_t M, const float* h,
+              const uint32_t* taus, size_t n_taus, std::vector<ViewSpec>* views,
+              std::vector<InstSpec>* insts) {
+  const size_t per_tau = M + M + M * (M - 1) / 2 + M * (M - 1);
+  insts->reserve(per_tau * n_taus);
+  for (size_t q = 0; q < n_taus; ++q) {
+    const uint32_t tau = taus[q];
+    const uint32_t n = (uint32_t)(n_rows - tau);
+    const uint32_t v0 = (uint32_t)views->size();
+    for (size_t j = 0; j < M; ++j) views->push_back({dc + j * n_rows, n});        // x_j[t]
+    for (size_t j = 0; j < M; ++j) views->push_back({dc + j * n_rows + tau, n});  // x_j[t+tau]
+    auto mk = [&](uint32_t d, uint32_t a, uint32_t b, uint32_t cc, float ha, float hb,
+                  float hc) {
+      InstSpec I;
+      I.d = d;
+      I.n = n;
+      I.view[0] = a;
+      I.view[1] = b;
+      I.view[2] = cc;
+      I.h[0] = ha;
+      I.h[1] = hb;
+      I.h[2] = hc;
+      I.norm = (double)n;
+      I.S = c.strip_subdiv;
+      insts->push_back(I);
+    };
+    for (size_t i = 0; i < M; ++i) mk(1, v0 + i, 0, 0, h[i], 1.f, 1.f);
+    for (size_t i = 0; i < M; ++i) mk(2, v0 + M + i, v0 + i, 0, h[i], h[i], 1.f);
+    for (size_t i = 0; i < M; ++i)
+      for (size_t j = i + 1; j < M; ++j) mk(2, v0 + i, v0 + j, 0, h[i], h[j], 1.f);
+    for (size_t i = 0; i < M; ++i)
+      for (size_t j = 0; j < M; ++j)
+        if (i != j) {
+          mk(3, v0 + M + i, v0 + i, v0 + j, h[i], h[i], h[j]);
+          // (y+, y, x): y follows the sorted y+ closely, so cells of h
+          // suffice there; x is independent and gets cells of h/2
+          // (3 x 5 strips; 3-D kernel on the 32 x 200k, 3-lag batch
+          // 815 -> 776 ms against 3 x 3)
+          insts->back().S3[0] = 1;
+          insts->back().S3[1] = 2;
+        }
+  }
+}
+
+// Keeps the listed instances (in the listed order) and the views they use.
+int select_items(Ctx& c, const uint64_t* items, size_t n_items, std::vector<ViewSpec>* views,
+                 std::vector<InstSpec>* insts) {
+  std::vector<InstSpec> sel;
+  sel.reserve(n_items);
+  std::vector<uint32_t> remap(views->size(), UINT32_MAX);
+  std::vector<ViewSpec> used;
+  for (size_t q = 0; q < n_items; ++q) {
+    if (items[q] >= insts->size()) return c.fail(ENT_ERR_ARG, "item index out of range");
+    InstSpec I = (*insts)[items[q]];
+    for (uint32_t j = 0; j < I.d; ++j) {
+      uint32_t& r = remap[I.view[j]];
+      if (r == UINT32_MAX) {
+        r = (uint32_t)used.size();
+        used.push_back((*views)[I.view[j]]);
+      }
+      I.view[j] = r;
+    }
+    sel.push_back(I);
+  }
+  *views = std::move(used);
+  *insts = std::move(sel);
+  return ENT_OK;
+}
+
 int mi_impl(ent_ctx* ctx, const float* coords, size_t n_rows, size_t n_cols,
             const float* h, uint32_t flags, double* mi_out, double* hx_out,
             bool device_in) {
@@ -76,33 +180,9 @@ int mi_impl(ent_ctx* ctx, const float* coords, size_t n_rows, size_t n_cols,
     if (e != cudaSuccess) return c.cuda_fail(e, "copy coordinates");
     dc = p;
   }
-  std::vector<ViewSpec> views(n_cols);
-  for (size_t j = 0; j < n_cols; ++j) views[j] = {dc + j * n_rows, (uint32_t)n_rows};
+  std::vector<ViewSpec> views;
   std::vector<InstSpec> insts;
-  insts.reserve(n_cols + n_cols * (n_cols - 1) / 2);
-  for (size_t i = 0; i < n_cols; ++i) {
-    InstSpec I;
-    I.d = 1;
-    I.n = (uint32_t)n_rows;
-    I.view[0] = (uint32_t)i;
-    I.h[0] = h[i];
-    I.norm = (double)n_rows;
-    I.S = c.strip_subdiv;
-    insts.push_back(I);
-  }
-  for (size_t i = 0; i < n_cols; ++i)
-    for (size_t j = i + 1; j < n_cols; ++j) {
-      InstSpec I;
-      I.d = 2;
-      I.n = (uint32_t)n_rows;
-      I.view[0] = (uint32_t)i;
-      I.view[1] = (uint32_t)j;
-      I.h[0] = h[i];
-      I.h[1] = h[j];
-      I.norm = (double)n_rows;
-      I.S = c.strip_subdiv;
-      insts.push_back(I);
-    }
+  mi_build(c, dc, n_rows, n_cols, h, &views, &insts);
   std::vector<double> H;
   const bool counts = (flags & ENT_BATCH_SUPPORT_COUNTS) != 0;
   s = run_entropies(c, views, insts, counts, &H);
@@ -153,48 +233,10 @@ int te_impl(ent_ctx* ctx, const float* coords, size_t n_rows, size_t n_cols, con
     dc = p;
   }
   const size_t M = n_cols;
+  const size_t per_tau = M + M + M * (M - 1) / 2 + M * (M - 1);
   std::vector<ViewSpec> views;
   std::vector<InstSpec> insts;
-  // index helpers: per lag, [M 1-D][M 2-D lag][M(M-1)/2 2-D joint][M(M-1) 3-D]
-  const size_t per_tau = M + M + M * (M - 1) / 2 + M * (M - 1);
-  insts.reserve(per_tau * n_taus);
-  for (size_t q = 0; q < n_taus; ++q) {
-    const uint32_t tau = taus[q];
-    const uint32_t n = (uint32_t)(n_rows - tau);
-    const uint32_t v0 = (uint32_t)views.size();
-    for (size_t j = 0; j < M; ++j) views.push_back({dc + j * n_rows, n});        // x_j[t]
-    for (size_t j = 0; j < M; ++j) views.push_back({dc + j * n_rows + tau, n});  // x_j[t+tau]
-    auto mk = [&](uint32_t d, uint32_t a, uint32_t b, uint32_t cc, float ha, float hb,
-                  float hc) {
-      InstSpec I;
-      I.d = d;
-      I.n = n;
-      I.view[0] = a;
-      I.view[1] = b;
-      I.view[2] = cc;
-      I.h[0] = ha;
-      I.h[1] = hb;
-      I.h[2] = hc;
-      I.norm = (double)n;
-      I.S = c.strip_subdiv;
-      insts.push_back(I);
-    };
-    for (size_t i = 0; i < M; ++i) mk(1, v0 + i, 0, 0, h[i], 1.f, 1.f);
-    for (size_t i = 0; i < M; ++i) mk(2, v0 + M + i, v0 + i, 0, h[i], h[i], 1.f);
-    for (size_t i = 0; i < M; ++i)
-      for (size_t j = i + 1; j < M; ++j) mk(2, v0 + i, v0 + j, 0, h[i], h[j], 1.f);
-    for (size_t i = 0; i < M; ++i)
-      for (size_t j = 0; j < M; ++j)
-        if (i != j) {
-          mk(3, v0 + M + i, v0 + i, v0 + j, h[i], h[i], h[j]);
-          // (y+, y, x): y follows the sorted y+ closely, so cells of h
-          // suffice there; x is independent and gets cells of h/2
-          // (3 x 5 strips; 3-D kernel on the 32 x 200k, 3-lag batch
-          // 815 -> 776 ms against 3 x 3)
-          insts.back().S3[0] = 1;
-          insts.back().S3[1] = 2;
-        }
-  }
+  te_build(c, dc, n_rows, M, h, taus, n_taus, &views, &insts);
   std::vector<double> H;
   const bool counts = (flags & ENT_BATCH_SUPPORT_COUNTS) != 0;
   s = run_entropies(c, views, insts, counts, &H);
@@ -250,6 +292,57 @@ int ent_mi_all_pairs_device(ent_ctx* ctx, const float* d_coords, size_t n_rows,
                             size_t n_cols, const float* h, uint32_t flags,
                             double* mi_out, double* h_out) {
   return mi_impl(ctx, d_coords, n_rows, n_cols, h, flags, mi_out, h_out, true);
+}
+
+// Entropies (or support counts) of listed densities of the MI or TE batch.
+static int items_impl(ent_ctx* ctx, bool te, const float* d_coords, size_t n_rows,
+                      size_t n_cols, const float* h, const uint32_t* taus, size_t n_taus,
+                      const uint64_t* items, size_t n_items, uint32_t flags, double* H_out) {
+  if (!ctx) return ENT_ERR_ARG;
+  Ctx& c = *reinterpret_cast<Ctx*>(ctx);
+  int s = c.begin_call();
+  if (s) return s;
+  if (!d_coords || !h || (!items && n_items) || (!H_out && n_items) || (te && (!taus || !n_taus)))
+    return c.fail(ENT_ERR_ARG, "null argument");
+  if (n_cols < 1 || n_rows < 1) return c.fail(ENT_ERR_ARG, "empty input");
+  if (n_rows > 0xffffff00ull) return c.fail(ENT_ERR_TOO_LARGE, "too many rows");
+  for (size_t j = 0; j < n_cols; ++j)
+    if (!(h[j] > 0.f) || !std::isfinite(h[j]))
+      return c.fail(ENT_ERR_ARG, "bandwidth must be finite and positive");
+  if (te)
+    for (size_t q = 0; q < n_taus; ++q)
+      if (taus[q] == 0 || taus[q] >= n_rows) return c.fail(ENT_ERR_ARG, "lag out of range");
+  std::vector<ViewSpec> views;
+  std::vector<InstSpec> insts;
+  if (te) te_build(c, d_coords, n_rows, n_cols, h, taus, n_taus, &views, &insts);
+  else mi_build(c, d_coords, n_rows, n_cols, h, &views, &insts);
+  s = select_items(c, items, n_items, &views, &insts);
+  if (s) return s;
+  std::vector<double> H;
+  if (n_items) {
+    s = run_entropies(c, views, insts, (flags & ENT_BATCH_SUPPORT_COUNTS) != 0, &H);
+    if (s) return s;
+  }
+  s = c.end_call();
+  c.collect_kernel_stats();
+  if (s) return s;
+  for (size_t q = 0; q < n_items; ++q) H_out[q] = H[q];
+  return ENT_OK;
+}
+
+int ent_mi_entropies_device(ent_ctx* ctx, const float* d_coords, size_t n_rows, size_t n_cols,
+                            const float* h, const uint64_t* items, size_t n_items,
+                            uint32_t flags, double* H_out) {
+  return items_impl(ctx, false, d_coords, n_rows, n_cols, h, nullptr, 0, items, n_items, flags,
+                    H_out);
+}
+
+int ent_te_entropies_device(ent_ctx* ctx, const float* d_coords, size_t n_rows, size_t n_cols,
+                            const float* h, const uint32_t* taus, size_t n_taus,
+                            const uint64_t* items, size_t n_items, uint32_t flags,
+                            double* H_out) {
+  return items_impl(ctx, true, d_coords, n_rows, n_cols, h, taus, n_taus, items, n_items, flags,
+                    H_out);
 }
 
 int ent_entropy_batch(ent_ctx* ctx, const ent_instance* inst, size_t n_inst,

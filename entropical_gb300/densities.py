@@ -264,6 +264,36 @@ class Context:
         self.check(st)
         return mi, hx
 
+    def mi_entropies_device(self, d_coords: int, n_rows: int, n_cols: int, h: Sequence[float],
+                            items: Sequence[int], counts: bool = False) -> np.ndarray:
+        """Entropies of the listed densities of the all-pairs MI batch (batch
+        order: the n_cols marginals, then the joints i < j in row order),
+        computed as one batch from device coordinates."""
+        hv = _f32(h)
+        it = np.ascontiguousarray(np.asarray(items, dtype=np.uint64))
+        out = np.zeros(len(it), dtype=np.float64)
+        self.check(self._lib.ent_mi_entropies_device(
+            self._h, C.c_void_p(d_coords), n_rows, n_cols, hv.ctypes.data_as(c_f32_p),
+            it.ctypes.data_as(C.POINTER(C.c_uint64)), len(it),
+            BATCH_SUPPORT_COUNTS if counts else 0, out.ctypes.data_as(c_f64_p)))
+        return out
+
+    def te_entropies_device(self, d_coords: int, n_rows: int, n_cols: int, h: Sequence[float],
+                            taus: Sequence[int], items: Sequence[int],
+                            counts: bool = False) -> np.ndarray:
+        """Entropies of the listed densities of the all-ordered-pairs TE batch
+        (batch order per lag: n_cols 1-D, n_cols lagged 2-D, the joints i < j,
+        the 3-D (i, j), i != j), computed as one batch from device
+        coordinates."""
+        hv, tv = _f32(h), _u32(taus)
+        it = np.ascontiguousarray(np.asarray(items, dtype=np.uint64))
+        out = np.zeros(len(it), dtype=np.float64)
+        self.check(self._lib.ent_te_entropies_device(
+            self._h, C.c_void_p(d_coords), n_rows, n_cols, hv.ctypes.data_as(c_f32_p),
+            tv.ctypes.data_as(c_u32_p), len(tv), it.ctypes.data_as(C.POINTER(C.c_uint64)),
+            len(it), BATCH_SUPPORT_COUNTS if counts else 0, out.ctypes.data_as(c_f64_p)))
+        return out
+
     def te_all_pairs(self, coords, h: Sequence[float], taus: Sequence[int],
                      counts: bool = False) -> np.ndarray:
         """All-ordered-pairs transfer entropy; returns (n_taus, M, M) with

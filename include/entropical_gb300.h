@@ -205,6 +205,28 @@ int ent_te_all_pairs_device(ent_ctx* ctx, const float* d_coords, size_t n_rows,
                             size_t n_cols, const float* h, const uint32_t* taus,
                             size_t n_taus, uint32_t flags, double* te_out);
 
+/*
+ * Entropies of a listed subset of the densities of the batches above, from
+ * device coordinates: the unit one rank computes when one MI or TE job is
+ * split over GPUs (the reference splits one density's target rows over its
+ * GPUs instead, density_1d.cuh:181-219; here whole densities are dealt out
+ * and each rank uploads the coordinate matrix once). items[q] is an index
+ * into the batch order -- for MI: 0..n_cols-1 the 1-D marginals, then the
+ * joints (i, j), i < j, in row order; for TE, per lag q in taus order:
+ * [n_cols 1-D y][n_cols 2-D (y+, y)][n_cols(n_cols-1)/2 2-D (y_i, x_j), i < j]
+ * [n_cols(n_cols-1) 3-D (y_i+, y_i, x_j), i != j, row order]. H_out[q]
+ * receives -mean log p of item q (with ENT_BATCH_SUPPORT_COUNTS, its
+ * in-support pair count). The listed densities run as one batch, and only
+ * the coordinate views they use are sorted. Outputs on the host.
+ */
+int ent_mi_entropies_device(ent_ctx* ctx, const float* d_coords, size_t n_rows, size_t n_cols,
+                            const float* h, const uint64_t* items, size_t n_items,
+                            uint32_t flags, double* H_out);
+int ent_te_entropies_device(ent_ctx* ctx, const float* d_coords, size_t n_rows, size_t n_cols,
+                            const float* h, const uint32_t* taus, size_t n_taus,
+                            const uint64_t* items, size_t n_items, uint32_t flags,
+                            double* H_out);
+
 /* One density instance of an uneven batch. */
 typedef struct {
   const float* coords; /* column-major d x n: dimension j at coords[j*n + i] */

@@ -87,12 +87,52 @@ def test_te_support_counts(ctx):
     assert cnt[0, 1, 2] == c.sum()
 
 
-def test_mi_split_form_matches_batch(ctx):
-    """The densities of one all-pairs MI dealt out as shares (here one rank)
-    through entropy batches give the MI batch's numbers."""
-    from entropical_gb300.replicas import mi_all_pairs_sharded
-    x = workloads.mi_coords(6000, 5, seed=21)
+@pytest.mark.parametrize("n_rows,n_cols", [(6000, 5), (100_000, 6)])
+def test_mi_split_over_ranks_matches_batch(ctx, n_rows, n_cols):
+    """One all-pairs MI dealt over three ranks (run here one after another on
+    one GPU, each share one batch from the same device matrix) gives the MI
+    batch's numbers; the shares hold every density once. The larger case
+    puts the joints on the strip moments."""
+    import torch
+    from entropical_gb300.replicas import WEIGHTS, deal, mi_assemble, mi_instances
+    x = workloads.mi_coords(n_rows, n_cols, seed=21)
     h = workloads.scott_bandwidth(x, 2)
-    mi_s, hx_s = mi_all_pairs_sharded(ctx.entropy_batch, x, h)
+    dx = torch.from_numpy(x).cuda()
+    inst = mi_instances(n_cols)
+    shares = deal([WEIGHTS[len(c)] for c in inst], 3)
+    assert sorted(int(i) for s in shares for i in s) == list(range(len(inst)))
+    H = np.zeros(len(inst))
+    for items in shares:
+        H[items] = ctx.mi_entropies_device(dx.data_ptr(), n_rows, n_cols, h, items)
+    mi_s, hx_s = mi_assemble(n_cols, H)
     mi, hx = ctx.mi_all_pairs(x, h)
     assert np.max(np.abs(mi_s - mi)) < 1e-7 and np.max(np.abs(hx_s - hx)) < 1e-7
+
+
+def test_te_split_over_ranks_matches_batch(ctx):
+    """The same for all-ordered-pairs TE at two lags."""
+    import torch
+    from entropical_gb300.replicas import WEIGHTS, deal, te_assemble, te_instances
+    x, _ = workloads.langevin(n_coords=4, n_steps=20_000, seed=8)
+    h = workloads.scott_bandwidth(x, 3)
+    taus = [1, 7]
+    dx = torch.from_numpy(np.ascontiguousarray(x)).cuda()
+    inst = te_instances(4, 2)
+    dim = {1: 1, 2: 2, 3: 2, 4: 3}
+    shares = deal([WEIGHTS[dim[k]] for _, k, _, _ in inst], 3)
+    H = np.zeros(len(inst))
+    for items in shares:
+        H[items] = ctx.te_entropies_device(dx.data_ptr(), x.shape[1], 4, h, taus, items)
+    te_s = te_assemble(4, 2, H)
+    te = ctx.te_all_pairs(x, h, taus)
+    assert np.max(np.abs(te_s - te)) < 1e-7
+
+
+def test_split_items_errors(ctx):
+    import torch
+    x = workloads.mi_coords(1000, 3, seed=2)
+    h = workloads.scott_bandwidth(x, 2)
+    dx = torch.from_numpy(x).cuda()
+    with pytest.raises(Exception):
+        ctx.mi_entropies_device(dx.data_ptr(), 1000, 3, h, [6])  # 3 + 3 densities: 0..5
+    assert len(ctx.mi_entropies_device(dx.data_ptr(), 1000, 3, h, [])) == 0

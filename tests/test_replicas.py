@@ -9,7 +9,8 @@ import pytest
 
 import numpy as np
 
-from entropical_gb300.replicas import aggregate, mi_all_pairs_sharded, mi_instances, shard
+from entropical_gb300.replicas import (WEIGHTS, aggregate, deal, mi_assemble, mi_instances, shard,
+                                       split_entropies, te_assemble, te_instances)
 
 
 def _free_port():
@@ -58,40 +59,75 @@ def test_shard_covers_everything_once():
             assert flat == list(range(n))
 
 
-def _fake_entropies(batch):
-    # any deterministic function of each instance stands in for the GPU batch
-    return [float(np.sum(x.astype(np.float64) ** 2) * float(np.prod(h))) + x.shape[0]
-            for x, h in batch]
+def _fake_entropies(items):
+    # any deterministic function of each item stands in for the GPU batch
+    return [np.sin(1.0 + float(i)) * 3.0 + 0.01 * float(i) for i in items]
 
 
-def _mi_worker(rank, world, port, out):
+def _split_worker(rank, world, port, out):
     import torch.distributed as dist
     os.environ["MASTER_ADDR"] = "127.0.0.1"
     os.environ["MASTER_PORT"] = str(port)
     dist.init_process_group("gloo", rank=rank, world_size=world)
-    x = np.random.default_rng(4).standard_normal((6, 50)).astype(np.float32)
-    h = [0.3, 0.4, 0.5, 0.6, 0.7, 0.8]
-    mi, hx = mi_all_pairs_sharded(_fake_entropies, x, h, dist)
-    out.put((rank, mi.tolist(), hx.tolist()))
+    w = [WEIGHTS[len(c)] for c in mi_instances(6)]
+    H = split_entropies(_fake_entropies, w, dist)
+    mi, hx = mi_assemble(6, H)
+    wt = [WEIGHTS[{1: 1, 2: 2, 3: 2, 4: 3}[k]] for _, k, _, _ in te_instances(4, 2)]
+    te = te_assemble(4, 2, split_entropies(_fake_entropies, wt, dist))
+    out.put((rank, mi.tolist(), hx.tolist(), te.tolist()))
     dist.barrier()
     dist.destroy_process_group()
 
 
-def test_mi_split_over_two_gloo_ranks():
+def test_split_over_two_gloo_ranks():
     mp = pytest.importorskip("torch.multiprocessing")
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     port = _free_port()
-    procs = [ctx.Process(target=_mi_worker, args=(r, 2, port, q)) for r in range(2)]
+    procs = [ctx.Process(target=_split_worker, args=(r, 2, port, q)) for r in range(2)]
     for p in procs:
         p.start()
     res = sorted(q.get(timeout=120) for _ in procs)
     for p in procs:
         p.join(timeout=60)
         assert p.exitcode == 0
-    x = np.random.default_rng(4).standard_normal((6, 50)).astype(np.float32)
-    h = [0.3, 0.4, 0.5, 0.6, 0.7, 0.8]
-    mi1, hx1 = mi_all_pairs_sharded(_fake_entropies, x, h)
-    for _, mi, hx in res:
+    w = [WEIGHTS[len(c)] for c in mi_instances(6)]
+    mi1, hx1 = mi_assemble(6, split_entropies(_fake_entropies, w))
+    wt = [WEIGHTS[{1: 1, 2: 2, 3: 2, 4: 3}[k]] for _, k, _, _ in te_instances(4, 2)]
+    te1 = te_assemble(4, 2, split_entropies(_fake_entropies, wt))
+    for _, mi, hx, te in res:
         assert np.array_equal(np.array(mi), mi1) and np.array_equal(np.array(hx), hx1)
+        assert np.array_equal(np.array(te), te1)
     assert len(mi_instances(64)) == 64 + 2016
+
+
+def test_deal_covers_everything_once_and_balances():
+    inst = mi_instances(64)
+    w = [WEIGHTS[len(c)] for c in inst]
+    for world in (1, 2, 3, 8):
+        shares = deal(w, world)
+        flat = sorted(int(i) for s in shares for i in s)
+        assert flat == list(range(len(inst)))
+        loads = [sum(w[int(i)] for i in s) for s in shares]
+        assert max(loads) - min(loads) <= max(w)
+        # the cheap marginals do not all land on one rank
+        if world > 1:
+            assert all(any(int(i) < 64 for i in s) for s in shares[:2]) or world > 64
+
+
+def test_te_assemble_formula():
+    M, T = 3, 2
+    inst = te_instances(M, T)
+    H = np.arange(len(inst), dtype=np.float64) * 0.5 + 1.0
+    te = te_assemble(M, T, H)
+    idx = {v: k for k, v in enumerate(inst)}
+    for q in range(T):
+        for i in range(M):
+            for j in range(M):
+                if i == j:
+                    assert te[q, i, j] == 0
+                    continue
+                a, b = min(i, j), max(i, j)
+                ref = (H[idx[(q, 3, a, b)]] + H[idx[(q, 2, i, i)]] - H[idx[(q, 4, i, j)]]
+                       - H[idx[(q, 1, i, i)]])
+                assert te[q, i, j] == ref
