@@ -720,12 +720,27 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
       return c.cuda_fail(es, "batch kernels");
     }
     if (e != cudaSuccess) return c.cuda_fail(e, "end capture");
-    cudaGraphExec_t ge = nullptr;
-    e = cudaGraphInstantiate(&ge, g, 0);
+    if (c.graph_exec) {
+      cudaGraphExecUpdateResultInfo info;
+      if (cudaGraphExecUpdate(c.graph_exec, g, &info) == cudaSuccess) {
+        ++c.graph_updates;
+      } else {  // another shape: instantiate this one
+        cudaGetLastError();
+        cudaGraphExecDestroy(c.graph_exec);
+        c.graph_exec = nullptr;
+      }
+    }
+    if (!c.graph_exec) {
+      e = cudaGraphInstantiate(&c.graph_exec, g, 0);
+      if (e != cudaSuccess) {
+        c.graph_exec = nullptr;
+        cudaGraphDestroy(g);
+        return c.cuda_fail(e, "graph instantiate");
+      }
+      ++c.graph_instantiations;
+    }
     cudaGraphDestroy(g);
-    if (e != cudaSuccess) return c.cuda_fail(e, "graph instantiate");
-    e = cudaGraphLaunch(ge, st);
-    cudaGraphExecDestroy(ge);
+    e = cudaGraphLaunch(c.graph_exec, st);
     if (e != cudaSuccess) return c.cuda_fail(e, "graph launch");
   } else {
     e = sequence();
@@ -823,6 +838,7 @@ void ent_destroy(ent_ctx* ctx) {
   Ctx* c = reinterpret_cast<Ctx*>(ctx);
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
+  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
   c->arena.release();
   cudaFree(c->d_err);
   if (c->d_logtab) cudaFree(c->d_logtab);

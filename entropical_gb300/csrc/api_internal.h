@@ -64,6 +64,12 @@ struct Ctx {
   bool moment_auto = true;
   uint32_t moment_cells = 3;  // strips per bandwidth of PAIR_MOMENT (2..12)
   bool use_graphs = true;       // capture the batch kernel sequence in a CUDA graph
+  // The batch's executable graph, kept across calls: a later batch is
+  // captured again and, when its kernel sequence has the same shape, the
+  // executable is updated in place (cudaGraphExecUpdate: new pointers, sizes
+  // and grids) instead of being instantiated anew.
+  cudaGraphExec_t graph_exec = nullptr;
+  uint32_t graph_updates = 0, graph_instantiations = 0;
 
   // grid of a persistent kernel: resident CTAs per SM x SMs, capped by work
   unsigned persistent_grid(uint32_t n_work, const void* kern, int threads, size_t smem);

@@ -136,3 +136,24 @@ def test_split_items_errors(ctx):
     with pytest.raises(Exception):
         ctx.mi_entropies_device(dx.data_ptr(), 1000, 3, h, [6])  # 3 + 3 densities: 0..5
     assert len(ctx.mi_entropies_device(dx.data_ptr(), 1000, 3, h, [])) == 0
+
+
+def test_graph_reuse_across_batches():
+    """One context keeps its batch graph: calls alternating between two batch
+    shapes (the graph updated in place or instantiated anew) give the same
+    numbers as a fresh context for each."""
+    from entropical_gb300 import Context
+    xa = workloads.mi_coords(8000, 5, seed=31)
+    ha = workloads.scott_bandwidth(xa, 2)
+    xb = workloads.mi_coords(5000, 7, seed=32)
+    hb = workloads.scott_bandwidth(xb, 2)
+    with Context(0) as fresh:
+        ref_a, _ = fresh.mi_all_pairs(xa, ha)
+    with Context(0) as fresh:
+        ref_b, _ = fresh.mi_all_pairs(xb, hb)
+    with Context(0) as c:
+        for _ in range(3):
+            mi_a, _ = c.mi_all_pairs(xa, ha)
+            mi_b, _ = c.mi_all_pairs(xb, hb)
+            assert np.max(np.abs(mi_a - ref_a)) < 1e-9
+            assert np.max(np.abs(mi_b - ref_b)) < 1e-9
