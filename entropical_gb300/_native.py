@@ -57,6 +57,8 @@ SIGNATURES: dict[str, tuple] = {
     "ent_set_tuning": (C.c_int, [C.c_void_p, C.c_void_p]),
     "ent_log64_selftest": (C.c_int, [C.c_void_p, c_f64_p, C.c_size_t, c_f64_p]),
     "ent_wait_selftest": (C.c_int, [C.c_void_p]),
+    "ent_ilog_selftest": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.c_size_t,
+                                    C.POINTER(C.c_int64)]),
     "ent_autotune": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_uint32, C.c_uint32,
                                C.c_void_p]),
     "ent_autotune_cache_size": (C.c_size_t, [C.c_void_p]),

@@ -145,6 +145,22 @@ cudaError_t init_log_table(double2** out) {
   return cudaMemcpy(*out, t.data(), sizeof(double2) * t.size(), cudaMemcpyHostToDevice);
 }
 
+// Table of the strip-moment epilogue's log (ilog_fx48, moments2d.cu): per
+// k, inv = 1/c rounded to FP32 for c = 1 + (k + 1/2)/256, and log(1/inv)
+// rounded to 2^-56, computed with the host's libm in long double.
+cudaError_t init_ilog_table(ILogEntry** out) {
+  std::vector<ILogEntry> t(ILOG_TABLE_ENTRIES);
+  for (int k = 0; k < ILOG_TABLE_ENTRIES; ++k) {
+    const long double c = 1.0L + ((long double)k + 0.5L) / 256.0L;
+    t[k].inv = (float)(1.0L / c);
+    t[k].pad = 0.f;
+    t[k].l56 = (long long)std::llround(-std::log((long double)t[k].inv) * 0x1p56L);
+  }
+  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(out), sizeof(ILogEntry) * t.size());
+  if (e != cudaSuccess) return e;
+  return cudaMemcpy(*out, t.data(), sizeof(ILogEntry) * t.size(), cudaMemcpyHostToDevice);
+}
+
 // ----------------------------------------------------------------- engine
 namespace {
 
@@ -559,6 +575,7 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
       m.out = hi[i].out;
       m.acc = hi[i].acc;
       m.scale = hi[i].scale;
+      m.logc = std::log(hi[i].scale) - 92.0 * std::log(2.0);
       m.slot_base = hi[i].tile_base;
       m.P = c.arena.alloc(moments2d_prefix_bytes(hi[i].n));
       if (!m.ybound || !m.P) return c.fail(ENT_ERR_CUDA, "out of device memory");
@@ -684,7 +701,7 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
                              tile_ls + group_base[2], mode, c.n_sms, &launched);
         if (r == cudaSuccess)
           r = launch_moments2d(st, dm2, (uint32_t)m2.size(), m2_max_n, m2_max_strips, dm2_blk,
-                               m2_blocks, m2_tot, c.d_logtab, tile_ls, mode);
+                               m2_blocks, m2_tot, c.d_ilogtab, tile_ls, mode);
         launches += 5;
       } else {
         r = launch_density(st, d, c.tile_r[d - 1], var_d[d], tiles + group_base[d],
@@ -829,6 +846,11 @@ int ent_create(ent_ctx** out, int device) {
     ent_destroy(reinterpret_cast<ent_ctx*>(c));
     return ENT_ERR_CUDA;
   }
+  if (init_ilog_table(&c->d_ilogtab) != cudaSuccess) {
+    cudaGetLastError();
+    ent_destroy(reinterpret_cast<ent_ctx*>(c));
+    return ENT_ERR_CUDA;
+  }
   *out = reinterpret_cast<ent_ctx*>(c);
   return ENT_OK;
 }
@@ -842,6 +864,7 @@ void ent_destroy(ent_ctx* ctx) {
   c->arena.release();
   cudaFree(c->d_err);
   if (c->d_logtab) cudaFree(c->d_logtab);
+  if (c->d_ilogtab) cudaFree(c->d_ilogtab);
   cudaEventDestroy(c->ev_call0);
   cudaEventDestroy(c->ev_call1);
   cudaEventDestroy(c->ev_k0);
@@ -895,6 +918,23 @@ int ent_log64_selftest(ent_ctx* ctx, const double* x, size_t n, double* out) {
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(out, d + n, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream);
   if (e != cudaSuccess) return c->cuda_fail(e, "log self-test");
+  return c->end_call();
+}
+
+int ent_ilog_selftest(ent_ctx* ctx, const uint64_t* t, size_t n, int64_t* out) {
+  if (!ctx || (n && (!t || !out))) return ENT_ERR_ARG;
+  Ctx* c = reinterpret_cast<Ctx*>(ctx);
+  int s = c->begin_call();
+  if (s) return s;
+  if (n == 0) return c->end_call();
+  unsigned long long* d = static_cast<unsigned long long*>(c->arena.alloc(24 * n));
+  if (!d) return c->fail(ENT_ERR_CUDA, "out of device memory");
+  long long* dout = reinterpret_cast<long long*>(d + 2 * n);
+  cudaError_t e = cudaMemcpyAsync(d, t, 16 * n, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = launch_ilog_test(c->stream, d, n, c->d_ilogtab, dout);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(out, dout, 8 * n, cudaMemcpyDeviceToHost, c->stream);
+  if (e != cudaSuccess) return c->cuda_fail(e, "ilog self-test");
   return c->end_call();
 }
 

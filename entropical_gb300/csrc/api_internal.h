@@ -10,6 +10,8 @@
 
 #include "../../include/entropical_gb300.h"
 
+namespace ent { struct ILogEntry; }
+
 // Grow-only device workspace. Blocks are kept across calls; when a call
 // needed more than one block, the next call coalesces them into one.
 struct Arena {
@@ -32,6 +34,7 @@ struct Ctx {
   cudaStream_t stream = nullptr;
   uint32_t* d_err = nullptr;
   double2* d_logtab = nullptr;  // LOG64_TABLE_ENTRIES entries of log_fp64
+  ent::ILogEntry* d_ilogtab = nullptr;  // table of the strip-moment epilogue's log
   cudaEvent_t ev_call0 = nullptr, ev_call1 = nullptr;
   cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr;
   cudaEvent_t ev_d[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};

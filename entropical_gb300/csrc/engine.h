@@ -193,6 +193,7 @@ struct Mom2D {
   double* out;                  // per-point density by original index (nullable)
   const double* acc;            // edge-strip sums by sorted position (InstDev::acc)
   double scale;                 // InstDev::scale
+  double logc;                  // log(scale) - 92 log 2 (the epilogue's offset)
   uint32_t n, n_strips, S;      // strips within S - 1 of a target's own are
                                 // summed here, those at S by the pair kernel
   float g2[2];
@@ -200,6 +201,16 @@ struct Mom2D {
   uint32_t blk_base;            // first target block of the instance
   uint32_t slot_base;           // first tile_logsum slot (one per target block)
 };
+// Table entry of the strip-moment epilogue's log (moments2d.cu): inv ~ 1/c,
+// c = 1 + (k + 1/2)/256, and log(1/inv) in 2^-56 fixed point.
+struct ILogEntry {
+  float inv;
+  float pad;
+  long long l56;
+};
+constexpr int ILOG_TABLE_ENTRIES = 256;
+cudaError_t launch_ilog_test(cudaStream_t st, const unsigned long long* t, size_t n,
+                             const ILogEntry* tab, long long* out);
 uint32_t moments2d_chunks(uint32_t n);
 uint32_t moments2d_blocks(uint32_t n);
 size_t moments2d_prefix_bytes(uint32_t n);
@@ -209,7 +220,7 @@ size_t moments2d_prefix_bytes(uint32_t n);
 // mode: the DM_* epilogue (no DM_COUNT)
 cudaError_t launch_moments2d(cudaStream_t st, const Mom2D* ms, uint32_t n_inst, uint32_t max_n,
                              uint32_t max_strips, const uint32_t* blk_base, uint32_t n_blocks,
-                             void* chunk_tot, const double2* logtab, double* tile_logsum,
+                             void* chunk_tot, const ILogEntry* ilog, double* tile_logsum,
                              uint32_t mode);
 // Mean in-support neighbours per target of 2-D instances, sampled: per
 // instance 32 targets at quantiles of dimension 0, each with its window

@@ -29,8 +29,10 @@
 // Fixed-point rounding of the coordinates (2^-23 g) changes a kernel value
 // by less than 2^-21 g^2 per dimension, far below the 1e-5 density bar.
 //
-// The epilogue (scale, per-point output, FP64 log and per-block sums) runs
-// in the same kernel; the symmetric kernel's finish skips these instances.
+// The epilogue (scale, per-point output, log and per-block sums) runs in the
+// same kernel; the symmetric kernel's finish skips these instances. The log
+// of each target's exact sum is taken in 64-bit fixed point (ilog_fx48) and
+// the block sums are exact integer sums.
 #include <algorithm>
 
 #include "engine.h"
@@ -164,6 +166,108 @@ __device__ __forceinline__ double s128_to_double(u128 v) {
   const double d = __ull2double_rn((unsigned long long)(v >> 64)) * 18446744073709551616.0 +
                    __ull2double_rn((unsigned long long)v);
   return neg ? -d : d;
+}
+
+// ---------------------------------------------- log of an exact 128-bit sum
+// The per-point log of the strip-moment epilogue without the FP64 pipe (it
+// runs at a small fraction of the FP32 rate on this GPU): the target's sum is
+// one exact nonnegative integer T (units of 2^-92 g^4), and log T is formed in
+// 64-bit fixed point with 2^-48 resolution. T = m 2^p with m in [1, 2) taken
+// from T's top 48 bits; the top 8 bits of m after the leading one pick a table
+// entry {inv ~ 1/c, log(1/inv) in 2^-56 fixed point}, c = 1 + (k + 1/2)/256
+// (the table is made on the host with its libm); r = m inv - 1 is formed
+// exactly as a float-float pair rh + rl (|r| < 2^-8, |rl| < 2^-22),
+// log1p(r) = r - r^2/2 + r^3/3 - r^4/4 + r^5/5 with rh^2 as an exact FP32
+// product pair and the rl cross terms to r^3, and
+//   log T = p ln 2 + log(1/inv) + log1p(r),
+// every part added in fixed point. Error below 2^-45 (2.9e-14) absolute: the
+// 48-bit truncation of T, the rounding of rl and of the fixed-point parts.
+constexpr int64_t LN2_FX56 = 49946518145322874LL;  // round(ln 2 * 2^56)
+
+// round(x 2^48) of a float with |x| < 1
+__device__ __forceinline__ int64_t f32_to_fx48(float x) {
+  const uint32_t b = __float_as_uint(x);
+  const int e = (int)((b >> 23) & 0xffu);
+  if (e == 0) return 0;
+  const int64_t m = (int64_t)((b & 0x7fffffu) | 0x800000u);
+  const int sh = e - 102;  // x 2^48 = m 2^(e - 150 + 48)
+  int64_t q;
+  if (sh >= 0) q = m << sh;
+  else if (sh > -25) q = (m + (1LL << (-sh - 1))) >> (-sh);
+  else q = 0;
+  return (b & 0x80000000u) ? -q : q;
+}
+
+// (hi, lo) += m 2^sh rounded to an integer, m < 2^53 (the fixed-point image
+// of a nonnegative float or double; two 64-bit words, no 128-bit shifts)
+__device__ __forceinline__ void add_shifted(uint64_t m, int sh, uint64_t& lo, uint64_t& hi) {
+  uint64_t a = 0, b = 0;  // low and high word of the addend
+  if (sh >= 64) {
+    b = m << (sh - 64);
+  } else if (sh > 0) {
+    a = m << sh;
+    b = m >> (64 - sh);
+  } else if (sh == 0) {
+    a = m;
+  } else if (sh > -54) {
+    a = (m + (1ull << (-sh - 1))) >> (-sh);
+  }
+  lo += a;
+  hi += b + (lo < a ? 1ull : 0ull);
+}
+
+// += round(v 2^92) for a finite float v >= 0 below 2^30
+__device__ __forceinline__ void add_fx92_f32(float v, uint64_t& lo, uint64_t& hi) {
+  const uint32_t b = __float_as_uint(v);
+  const int e = (int)((b >> 23) & 0xffu);
+  if (e == 0 || (b >> 31)) return;
+  add_shifted((uint64_t)((b & 0x7fffffu) | 0x800000u), e - 150 + 92, lo, hi);
+}
+
+// += round(v 2^92) for a finite double v >= 0 below 2^30
+__device__ __forceinline__ void add_fx92_f64(double v, uint64_t& lo, uint64_t& hi) {
+  const uint64_t b = (uint64_t)__double_as_longlong(v);
+  const int e = (int)((b >> 52) & 0x7ffu);
+  if (e == 0 || (b >> 63)) return;
+  add_shifted((b & 0xfffffffffffffull) | (1ull << 52), e - 1075 + 92, lo, hi);
+}
+
+// log(T) in 2^-48 fixed point of T = hi 2^64 + lo > 0
+__device__ __forceinline__ int64_t ilog_fx48(uint64_t lo, uint64_t hi,
+                                             const ILogEntry* __restrict__ tab) {
+  if ((lo | hi) == 0) return -(1LL << 62);  // never for a density: its own term is > 0
+  const int p = hi ? 127 - __clzll((long long)hi) : 63 - __clzll((long long)lo);
+  const int s = p - 47;  // m48 = floor(T / 2^s), in [2^47, 2^48)
+  uint64_t m48;
+  if (s >= 64) m48 = hi >> (s - 64);
+  else if (s > 0) m48 = (hi << (64 - s)) | (lo >> s);
+  else m48 = lo << (-s);
+  const uint32_t k = (uint32_t)(m48 >> 39) & 255u;
+  const ILogEntry t = tab[k];
+  // m = mh + ml exactly (24 + 24 bits)
+  const float mh = __uint_as_float(0x3f800000u | (uint32_t)((m48 >> 24) & 0x7fffffu));
+  const float ml = __fmul_rn(__uint2float_rn((uint32_t)(m48 & 0xffffffu)), 0x1p-47f);
+  const float p1 = __fmul_rn(mh, t.inv);
+  const float e1 = __fmaf_rn(mh, t.inv, -p1);  // mh inv = p1 + e1 exactly
+  const float rh = __fsub_rn(p1, 1.0f);        // exact: p1 in [1/2, 2]
+  const float rl = __fmaf_rn(ml, t.inv, e1);
+  const float qh = __fmul_rn(rh, rh);
+  const float qe = __fmaf_rn(rh, rh, -qh);     // rh^2 = qh + qe exactly
+  // two-sum of rh and -qh/2
+  const float b2 = __fmul_rn(-0.5f, qh);
+  const float sh = __fadd_rn(rh, b2);
+  const float bb = __fsub_rn(sh, rh);
+  const float err = __fadd_rn(__fsub_rn(rh, __fsub_rn(sh, bb)), __fsub_rn(b2, bb));
+  const float h3 = __fmul_rn(__fmul_rn(rh, qh),
+                             __fmaf_rn(rh, __fmaf_rn(rh, 0.2f, -0.25f), 1.0f / 3.0f));
+  // the small rest: rounding of the two-sum and the cross terms of r^2/2 and
+  // r^3/3 with rl (-rh rl + rh^2 rl); rl itself is added on its own
+  const float rest = __fadd_rn(__fadd_rn(err, __fmaf_rn(-0.5f, qe, h3)),
+                               __fmul_rn(rl, __fsub_rn(qh, rh)));
+  int64_t fx = ((int64_t)p * LN2_FX56 + 128) >> 8;
+  fx += (t.l56 + 128) >> 8;
+  fx += f32_to_fx48(sh) + f32_to_fx48(rl) + f32_to_fx48(rest);
+  return fx;
 }
 
 // y extent (smallest, largest scaled y) of every strip: one warp per strip
@@ -374,11 +478,15 @@ constexpr int M2_MAX_IN = 23;  // inside strips per target: 2S - 1, S <= 12
 // Epilogue as the other bodies' finish kernel: density = scale x sum,
 // written by original index and/or logged (FP64) and summed per block of
 // targets in a fixed order into the instance's slots of tile_logsum.
+// LOGONLY: the log-sum epilogue alone (mode == DM_LOGSUM, the estimator
+// batches), compiled without the FP64 density path of the other modes.
+template <bool LOGONLY>
 __global__ void __launch_bounds__(M2_TB, 10)
     k_m2_density(const Mom2D* __restrict__ ms, uint32_t n_inst,
-                 const uint32_t* __restrict__ blk_base, const double2* __restrict__ logtab,
+                 const uint32_t* __restrict__ blk_base, const ILogEntry* __restrict__ ilog,
                  double* __restrict__ tile_logsum, uint32_t mode) {
   __shared__ double s_part[M2_TB / 32];
+  __shared__ long long s_fx[M2_TB / 32];
   __shared__ uint32_t s_br[M2_TB / 32][4 * M2_MAX_IN];
   const uint32_t gb = blockIdx.x;
   uint32_t lo = 0, hi = n_inst;
@@ -456,7 +564,8 @@ __global__ void __launch_bounds__(M2_TB, 10)
       fs += a0 + a1;
     }
   }
-  double v = 0.0;  // this target's term of the block sum
+  double v = 0.0;     // DM_SUMV: this target's density
+  long long fx = 0;   // DM_LOGSUM: log of this target's sum, 2^-48 fixed point
   if (valid) {
     // sum_b d_b M_ab for a = 0, 1, 2 (d_2 = -1), then sum_a c_a (.) (c_2 = -1)
     const u128 TX = quant<23>(t.x), TY = quant<23>(t.y);
@@ -465,16 +574,31 @@ __global__ void __launch_bounds__(M2_TB, 10)
     const u128 e0 = d0 * (u128)cnt + d1 * mo[1] - mo[4];
     const u128 e1 = d0 * mo[0] + d1 * mo[3] - mo[6];
     const u128 e2 = d0 * mo[2] + d1 * mo[5] - mo[7];
-    const u128 ex = c0 * e0 + c1 * e1 - e2;
-    // 2^-92 converts the fixed-point products back to units of g^4
-    double sum = s128_to_double(ex) * 0x1p-92 + (double)fs;
-    if (M.acc) sum += M.acc[k];
-    const double dens = M.scale * sum;
-    if (mode & DM_WRITE_F64) M.out[M.perm[k]] = dens;
-    if (mode & DM_LOGSUM) v = log_fp64(dens, logtab);
-    else if (mode & DM_SUMV) v = dens;
+    // the whole sum in units of 2^-92 g^4: the exact moment part, the
+    // partial strips' and the edge strips' sums in fixed point
+    const u128 T = c0 * e0 + c1 * e1 - e2;
+    uint64_t tlo = (uint64_t)T, thi = (uint64_t)(T >> 64);
+    if (fs != 0.f) add_fx92_f32(fs, tlo, thi);
+    if (M.acc) add_fx92_f64(M.acc[k], tlo, thi);
+    if (!LOGONLY && (mode & (DM_WRITE_F64 | DM_SUMV))) {
+      const double dens = M.scale * (s128_to_double(((u128)thi << 64) | tlo) * 0x1p-92);
+      if (mode & DM_WRITE_F64) M.out[M.perm[k]] = dens;
+      v = dens;
+    }
+    if (mode & DM_LOGSUM) fx = ilog_fx48(tlo, thi, ilog);
   }
-  if (mode & (DM_LOGSUM | DM_SUMV)) {  // block-uniform
+  if (mode & DM_LOGSUM) {  // block-uniform: exact integer block sum
+    for (int o = 16; o; o >>= 1) fx += __shfl_xor_sync(FULL_MASK, fx, o);
+    if (lane == 0) s_fx[warp] = fx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      long long tsum = 0;
+      for (uint32_t w = 0; w < M2_TB / 32; ++w) tsum += s_fx[w];
+      const uint32_t nv = min(M2_TB, M.n - blk * M2_TB);
+      // log density = log T + log(scale) - 92 log 2 = log T + M.logc
+      tile_logsum[M.slot_base + blk] = (double)tsum * 0x1p-48 + (double)nv * M.logc;
+    }
+  } else if (!LOGONLY && (mode & DM_SUMV)) {
     for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(FULL_MASK, v, o);
     if (lane == 0) s_part[warp] = v;
     __syncthreads();
@@ -484,6 +608,14 @@ __global__ void __launch_bounds__(M2_TB, 10)
       tile_logsum[M.slot_base + blk] = tsum;
     }
   }
+}
+
+// Self-test of ilog_fx48 on 128-bit inputs given as (low, high) words.
+__global__ void k_ilog_test(const unsigned long long* __restrict__ t, size_t n,
+                            const ILogEntry* __restrict__ tab, long long* __restrict__ out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    out[i] = ilog_fx48(t[2 * i], t[2 * i + 1], tab);
 }
 
 // One warp per instance; lane l samples the target at quantile (2l+1)/64 of
@@ -537,7 +669,7 @@ size_t moments2d_prefix_bytes(uint32_t n) { return (size_t)NM * 16 * ((size_t)n 
 
 cudaError_t launch_moments2d(cudaStream_t st, const Mom2D* ms, uint32_t n_inst, uint32_t max_n,
                              uint32_t max_strips, const uint32_t* blk_base, uint32_t n_blocks,
-                             void* chunk_tot, const double2* logtab, double* tile_logsum,
+                             void* chunk_tot, const ILogEntry* ilog, double* tile_logsum,
                              uint32_t mode) {
   if (n_inst == 0 || n_blocks == 0) return cudaSuccess;
   u128* tot = static_cast<u128*>(chunk_tot);
@@ -546,7 +678,20 @@ cudaError_t launch_moments2d(cudaStream_t st, const Mom2D* ms, uint32_t n_inst, 
   k_m2_totals<<<gc, M2_PT, 0, st>>>(ms, tot);
   k_m2_chunks<<<(n_inst + 3) / 4, 128, 0, st>>>(ms, n_inst, tot);
   k_m2_write<<<gc, M2_PT, 0, st>>>(ms, tot);
-  k_m2_density<<<n_blocks, M2_TB, 0, st>>>(ms, n_inst, blk_base, logtab, tile_logsum, mode);
+  if (mode == DM_LOGSUM)
+    k_m2_density<true><<<n_blocks, M2_TB, 0, st>>>(ms, n_inst, blk_base, ilog, tile_logsum,
+                                                   mode);
+  else
+    k_m2_density<false><<<n_blocks, M2_TB, 0, st>>>(ms, n_inst, blk_base, ilog, tile_logsum,
+                                                    mode);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ilog_test(cudaStream_t st, const unsigned long long* t, size_t n,
+                             const ILogEntry* tab, long long* out) {
+  if (n == 0) return cudaSuccess;
+  const unsigned blocks = (unsigned)std::min<size_t>((n + 255) / 256, 4096);
+  k_ilog_test<<<blocks, 256, 0, st>>>(t, n, tab, out);
   return cudaGetLastError();
 }
 

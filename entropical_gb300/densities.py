@@ -405,6 +405,20 @@ class Context:
                                                  out.ctypes.data_as(c_f64_p)))
         return out
 
+    def ilog_selftest(self, values) -> np.ndarray:
+        """The strip-moment epilogue's log of nonnegative integers below 2^128
+        evaluated on the device: round(log(T) 2^48) per value (int64)."""
+        vals = [int(v) for v in values]
+        t = np.zeros(2 * len(vals), dtype=np.uint64)
+        for i, v in enumerate(vals):
+            t[2 * i] = v & 0xFFFFFFFFFFFFFFFF
+            t[2 * i + 1] = v >> 64
+        out = np.zeros(len(vals), dtype=np.int64)
+        self.check(self._lib.ent_ilog_selftest(self._h, t.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                               len(vals),
+                                               out.ctypes.data_as(C.POINTER(C.c_int64))))
+        return out
+
     def reference_estimator_device(self, d_coords: int, n_rows: int, n_cols: int,
                                    h: Sequence[float], estimator: int, tau: int = 0
                                    ) -> np.ndarray:

@@ -113,6 +113,13 @@ int ent_set_tuning(ent_ctx* ctx, const ent_tuning* tuning);
  * (a table-reduction log with few FP64 operations), on the device, for n
  * host values. No counterpart in the reference. */
 int ent_log64_selftest(ent_ctx* ctx, const double* x, size_t n, double* out);
+/*
+ * Self-test of the log the strip-moment epilogue takes of a density's exact
+ * 128-bit integer sum T (in 64-bit fixed point, FP32 arithmetic only): t holds
+ * n values as (low, high) 64-bit word pairs; out[i] = log(T_i) 2^48 within
+ * 8 (2^-45 absolute). No counterpart in the reference.
+ */
+int ent_ilog_selftest(ent_ctx* ctx, const uint64_t* t, size_t n, int64_t* out);
 /* Diagnostic of the failure path: one device-side wait that nothing
  * completes runs into its bound (2 s) and the call returns ENT_ERR_TIMEOUT;
  * the context stays usable. No counterpart in the reference. */

@@ -227,3 +227,24 @@ def test_bounded_wait_reports_timeout():
         x = np.random.default_rng(3).standard_normal((2, 2000)).astype(np.float32)
         p = c.combined_densities(x, None, [0, 1], [0.3, 0.3])
         assert rel_err(p, O.density_fp64(x, [0.3, 0.3])) < REL
+
+
+def test_integer_log_of_exact_sums(ctx):
+    """The strip-moment epilogue's log of an exact 128-bit sum, in 2^-48 fixed
+    point, against a 40-digit decimal log: within 2^-45 (2.9e-14) absolute."""
+    from decimal import Decimal, getcontext
+    getcontext().prec = 40
+    rng = np.random.default_rng(17)
+    vals = [1, 2, 3, 2 ** 47, 2 ** 47 + 1, 2 ** 92, 3 * 2 ** 90, 2 ** 127 - 1, 2 ** 64 - 1,
+            2 ** 64, 10 ** 30]
+    for bits in (20, 47, 48, 60, 64, 80, 92, 100, 110, 120, 127):
+        vals += [int(rng.integers(1 << 30)) << max(0, bits - 30) | int(rng.integers(1 << 20))
+                 for _ in range(40)]
+    # values right at the table's cell edges (top 8 bits after the leading one)
+    for k in range(0, 256, 5):
+        vals.append((256 + k) << 84)
+        vals.append(((256 + k) << 84) - 1)
+    out = ctx.ilog_selftest(vals)
+    for v, o in zip(vals, out):
+        ref = Decimal(v).ln() * (Decimal(2) ** 48)
+        assert abs(Decimal(int(o)) - ref) <= 8, (v, int(o), ref)  # 2^-45
