@@ -142,14 +142,14 @@ def fp32_peak_tflops(n_sms: int) -> tuple[float, str]:
                   "(no measured FP32 figure in MEASURED_PEAKS.json)")
 
 
-# Compulsory HBM bytes per 2-D point of the strip-moment kernels (one MI
-# step, log-sum epilogue): the point (8 B) read by the strip-extent,
-# moment-total, prefix-write and target kernels (4 x 8), the 128 B moment
-# prefix row written once, the strip key and the original index (4 + 4).
-# The target kernel re-reads only the rows at range ends, mostly from L2.
-MOMENT_BYTES_PER_POINT = 4 * 8 + 128 + 4 + 4
-
-
+# Compulsory HBM bytes per 2-D point of the strip-moment group (one MI step,
+# log-sum epilogue): the point (8 B) read by the strip-extent, moment-total,
+# prefix-write and target kernels (4 x 8) and by the edge kernel as a source
+# and as a target (2 x 8), the 128 B moment prefix row written once, the strip
+# key (4 B), and the FP64 edge sum written by the edge kernel and read by the
+# target kernel (2 x 8). The target kernel re-reads the rows at its range
+# ends from L2 (measured: 34 B per target from DRAM in all).
+MOMENT_BYTES_PER_POINT = 4 * 8 + 2 * 8 + 128 + 4 + 2 * 8
 def profile_figure(name: str, key: str) -> float | None:
     """A figure `key = value` from a committed ncu summary under profiles/."""
     p = ROOT / "profiles" / name
@@ -172,23 +172,44 @@ def hbm_peak_gbs() -> tuple[float, str]:
         return 6800.0, "fallback 6.8 TB/s (no MEASURED_PEAKS.json)"
 
 
-def moment_roofline(t2: float, points_2d: int) -> dict:
-    """Roofline of the 2-D strip-moment kernels (strip extents, moment
-    prefix sums, per-target range sums): algorithmic HBM bytes over their
-    CUDA-event time, against the measured copy bandwidth. They are bound by
-    load latency (binary-search probes, 128-bit moment rows from L1/L2), not
-    by HBM; the committed ncu summary gives the issue rate they reach."""
+def moment_roofline(t_target: float, t_edge: float, t2: float, points_2d: int,
+                    edge_pairs: float) -> dict:
+    """Roofline of the 2-D strip-moment group of the MI step (edge kernel,
+    strip extents, moment prefix sums, target kernel; CUDA events on the
+    library stream): compulsory HBM bytes over the group's time, against the
+    measured copy bandwidth, with the DRAM bytes ncu measured for the same
+    kernels (small case, scaled by points). Beside it, each of the two largest
+    kernels timed on its own: the target kernel k_m2_density (dominant;
+    dependent L1/L2 loads of the binary searches and 128-bit moment rows) and
+    the symmetric edge kernel (12 flops per candidate pair against the FP32
+    peak), with their ncu issue and FMA-pipe fractions."""
+    import torch
     peak, note = hbm_peak_gbs()
     achieved = MOMENT_BYTES_PER_POINT * points_2d / t2 / 1e9
     prof = "moments2d_mi64x100k_ncu.md"
+    fpeak, fnote = fp32_peak_tflops(torch.cuda.get_device_properties(0).multi_processor_count)
+    edge_tflops = 12.0 * edge_pairs / t_edge / 1e12
+    per_pt = profile_figure(prof, "dram_bytes_per_point")
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak,
-            "traffic": profile_figure(prof, "dram_bytes_per_step"),
-            "kernel": "k_m2_* (2-D strip moments: k_m2_density + prefix kernels)",
+            "traffic": per_pt * points_2d if per_pt else None,
+            "kernel": "2-D strip-moment group: k_m2_density, k_density_sym (edge strips), "
+                      "k_m2_write, k_m2_totals, k_m2_ybounds, k_m2_chunks",
             "bytes_per_point": MOMENT_BYTES_PER_POINT, "points_2d": points_2d,
-            "peak_kind": note,
-            "issue_frac_ncu": profile_figure(prof, "issue_frac"),
-            "note": "load-latency bound gather; see issue_frac_ncu and the profile"}
+            "group_ms": t2 * 1e3, "peak_kind": note,
+            "target_kernel": {"kernel": "k_m2_density", "ms": t_target * 1e3,
+                              "share_of_group": t_target / t2,
+                              "issue_frac_ncu": profile_figure(prof, "issue_frac"),
+                              "dram_bytes_per_target_ncu":
+                                  profile_figure(prof, "target_dram_bytes_per_target"),
+                              "bound": "dependent L1/L2 loads (long-scoreboard stalls)"},
+            "edge_kernel": {"kernel": "k_density_sym<2,32,4,4> (edge strips)",
+                            "ms": t_edge * 1e3, "share_of_group": t_edge / t2,
+                            "candidate_pairs": edge_pairs,
+                            "achieved_tflops": edge_tflops, "peak_tflops": fpeak,
+                            "frac": edge_tflops / fpeak,
+                            "fma_pipe_frac_ncu": profile_figure(prof, "edge_fma_pipe_frac"),
+                            "peak_kind": fnote}}
 
 
 def roofline_3d(pairs: float, ms: float) -> dict:
@@ -209,7 +230,7 @@ def roofline_3d(pairs: float, ms: float) -> dict:
 def ncu_traffic() -> float | None:
     """DRAM bytes per launch of the 2-D pair kernel from the committed ncu
     summary (profiles/), if one has been captured."""
-    p = ROOT / "profiles" / "density2d_mi64x100k_ncu.txt"
+    p = ROOT / "profiles" / "density2d_sym_mi8x100k_ncu.md"
     if not p.exists():
         return None
     for ln in p.read_text().splitlines():
@@ -725,6 +746,7 @@ def main():
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
 
     step_ms, k2_ms, k2_pairs, k1_ms, launches = [], [], [], [], 0
+    km_ms, ke_ms = [], []
     barrier()
     wall0 = time.perf_counter()
     with ClockSampler(local) as clk:
@@ -737,6 +759,8 @@ def main():
             k2_ms.append(st.pair_kernel_ms_by_dim[1])
             k1_ms.append(st.pair_kernel_ms_by_dim[0])
             k2_pairs.append(st.candidate_pairs_by_dim[1])
+            km_ms.append(st.moment_target_ms)
+            ke_ms.append(st.moment_edge_ms)
             launches += st.kernel_launches
     barrier()
     wall = time.perf_counter() - wall0
@@ -763,7 +787,8 @@ def main():
         return
     t2 = statistics.mean(k2_ms) / 1e3
     if var2 == 7:
-        roofline = moment_roofline(t2, M * (M - 1) // 2 * N_FRAMES)
+        roofline = moment_roofline(statistics.mean(km_ms) / 1e3, statistics.mean(ke_ms) / 1e3,
+                                   t2, M * (M - 1) // 2 * N_FRAMES, statistics.mean(k2_pairs))
     else:
         peak, peak_note = fp32_peak_tflops(n_sms)
         # symmetric bodies (4, 5) evaluate each unordered pair once and add it

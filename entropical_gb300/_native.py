@@ -31,6 +31,8 @@ class CallStats(C.Structure):
         ("total_ms", C.c_float),
         ("candidate_pairs_by_dim", C.c_uint64 * 3),
         ("pair_kernel_ms_by_dim", C.c_float * 3),
+        ("moment_target_ms", C.c_float),
+        ("moment_edge_ms", C.c_float),
     ]
 
 

@@ -695,13 +695,21 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
         // add the edge sums and write the slots of their instances (the rest
         // of those instances' slots stay zero).
         r = cudaMemsetAsync(tile_ls + group_base[2], 0, sizeof(double) * group_slots[2], st);
+        if (r == cudaSuccess) r = rec(c.ev_m[0][0]);
         if (r == cudaSuccess)
           r = launch_density(st, 2, c.tile_r[1], PAIR_SYM, tiles + group_base[2],
                              group_slots[2], di_sorted, wc + 2, c.d_err,
                              tile_ls + group_base[2], mode, c.n_sms, &launched);
+        if (r == cudaSuccess) r = rec(c.ev_m[0][1]);
         if (r == cudaSuccess)
-          r = launch_moments2d(st, dm2, (uint32_t)m2.size(), m2_max_n, m2_max_strips, dm2_blk,
-                               m2_blocks, m2_tot, c.d_ilogtab, tile_ls, mode);
+          r = launch_moments2d_prefix(st, dm2, (uint32_t)m2.size(), m2_max_n, m2_max_strips,
+                                      m2_tot);
+        if (r == cudaSuccess) r = rec(c.ev_m[1][0]);
+        if (r == cudaSuccess)
+          r = launch_moments2d_targets(st, dm2, (uint32_t)m2.size(), dm2_blk, m2_blocks,
+                                       c.d_ilogtab, tile_ls, mode);
+        if (r == cudaSuccess) r = rec(c.ev_m[1][1]);
+        c.ran_m = true;
         launches += 5;
       } else {
         r = launch_density(st, d, c.tile_r[d - 1], var_d[d], tiles + group_base[d],
@@ -791,6 +799,12 @@ unsigned Ctx::persistent_grid(uint32_t n_work, const void* kern, int threads, si
 void Ctx::collect_kernel_stats() {
   float ms = 0.f;
   if (cudaEventElapsedTime(&ms, ev_k0, ev_k1) == cudaSuccess) stats.pair_kernel_ms = ms;
+  if (ran_m) {
+    if (cudaEventElapsedTime(&ms, ev_m[0][0], ev_m[0][1]) == cudaSuccess) stats.moment_edge_ms = ms;
+    if (cudaEventElapsedTime(&ms, ev_m[1][0], ev_m[1][1]) == cudaSuccess)
+      stats.moment_target_ms = ms;
+    ran_m = false;
+  }
   for (int d = 0; d < 3; ++d) {
     if (ran_d[d] && cudaEventElapsedTime(&ms, ev_d[d][0], ev_d[d][1]) == cudaSuccess)
       stats.pair_kernel_ms_by_dim[d] = ms;
@@ -834,6 +848,10 @@ int ent_create(ent_ctx** out, int device) {
       cudaEventCreate(&c->ev_d[1][1]) != cudaSuccess ||
       cudaEventCreate(&c->ev_d[2][0]) != cudaSuccess ||
       cudaEventCreate(&c->ev_d[2][1]) != cudaSuccess ||
+      cudaEventCreate(&c->ev_m[0][0]) != cudaSuccess ||
+      cudaEventCreate(&c->ev_m[0][1]) != cudaSuccess ||
+      cudaEventCreate(&c->ev_m[1][0]) != cudaSuccess ||
+      cudaEventCreate(&c->ev_m[1][1]) != cudaSuccess ||
       cudaDeviceGetAttribute(&c->n_sms, cudaDevAttrMultiProcessorCount, device) !=
           cudaSuccess) {
     cudaGetLastError();
@@ -872,6 +890,10 @@ void ent_destroy(ent_ctx* ctx) {
   for (int d = 0; d < 3; ++d) {
     cudaEventDestroy(c->ev_d[d][0]);
     cudaEventDestroy(c->ev_d[d][1]);
+  }
+  for (int k = 0; k < 2; ++k) {
+    cudaEventDestroy(c->ev_m[k][0]);
+    cudaEventDestroy(c->ev_m[k][1]);
   }
   cudaStreamDestroy(c->stream);
   delete c;

@@ -39,6 +39,9 @@ struct Ctx {
   cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr;
   cudaEvent_t ev_d[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
   bool ran_d[3] = {false, false, false};
+  // strip moments: edge (symmetric) kernel and target kernel
+  cudaEvent_t ev_m[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  bool ran_m = false;
   uint64_t h_nsrc_d[3] = {0, 0, 0};
   Arena arena;
   std::string last_error;

@@ -214,14 +214,14 @@ cudaError_t launch_ilog_test(cudaStream_t st, const unsigned long long* t, size_
 uint32_t moments2d_chunks(uint32_t n);
 uint32_t moments2d_blocks(uint32_t n);
 size_t moments2d_prefix_bytes(uint32_t n);
-// ms: 2-D instances in ascending blk_base; chunk_tot: 128 B per chunk;
-// mode: the DM_* epilogue (no DM_COUNT)
-// ms: 2-D instances in ascending blk_base; chunk_tot: 128 B per chunk;
-// mode: the DM_* epilogue (no DM_COUNT)
-cudaError_t launch_moments2d(cudaStream_t st, const Mom2D* ms, uint32_t n_inst, uint32_t max_n,
-                             uint32_t max_strips, const uint32_t* blk_base, uint32_t n_blocks,
-                             void* chunk_tot, const ILogEntry* ilog, double* tile_logsum,
-                             uint32_t mode);
+// The strip extents and moment prefix sums (four kernels), then the target
+// kernel with its epilogue. ms: 2-D instances in ascending blk_base;
+// chunk_tot: 128 B per chunk; mode: the DM_* epilogue (no DM_COUNT).
+cudaError_t launch_moments2d_prefix(cudaStream_t st, const Mom2D* ms, uint32_t n_inst,
+                                    uint32_t max_n, uint32_t max_strips, void* chunk_tot);
+cudaError_t launch_moments2d_targets(cudaStream_t st, const Mom2D* ms, uint32_t n_inst,
+                                     const uint32_t* blk_base, uint32_t n_blocks,
+                                     const ILogEntry* ilog, double* tile_logsum, uint32_t mode);
 // Mean in-support neighbours per target of 2-D instances, sampled: per
 // instance 32 targets at quantiles of dimension 0, each with its window
 // count in dimension 0 times the y-support fraction of up to 32 window points.

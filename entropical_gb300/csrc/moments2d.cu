@@ -667,17 +667,22 @@ uint32_t moments2d_blocks(uint32_t n) { return (n + M2_TB - 1) / M2_TB; }
 uint32_t moments2d_block_targets() { return M2_TB; }
 size_t moments2d_prefix_bytes(uint32_t n) { return (size_t)NM * 16 * ((size_t)n + 1); }
 
-cudaError_t launch_moments2d(cudaStream_t st, const Mom2D* ms, uint32_t n_inst, uint32_t max_n,
-                             uint32_t max_strips, const uint32_t* blk_base, uint32_t n_blocks,
-                             void* chunk_tot, const ILogEntry* ilog, double* tile_logsum,
-                             uint32_t mode) {
-  if (n_inst == 0 || n_blocks == 0) return cudaSuccess;
+cudaError_t launch_moments2d_prefix(cudaStream_t st, const Mom2D* ms, uint32_t n_inst,
+                                    uint32_t max_n, uint32_t max_strips, void* chunk_tot) {
+  if (n_inst == 0) return cudaSuccess;
   u128* tot = static_cast<u128*>(chunk_tot);
   k_m2_ybounds<<<dim3((max_strips + 7) / 8, n_inst), 256, 0, st>>>(ms);
   const dim3 gc(moments2d_chunks(std::max(max_n, 1u)), n_inst);
   k_m2_totals<<<gc, M2_PT, 0, st>>>(ms, tot);
   k_m2_chunks<<<(n_inst + 3) / 4, 128, 0, st>>>(ms, n_inst, tot);
   k_m2_write<<<gc, M2_PT, 0, st>>>(ms, tot);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_moments2d_targets(cudaStream_t st, const Mom2D* ms, uint32_t n_inst,
+                                     const uint32_t* blk_base, uint32_t n_blocks,
+                                     const ILogEntry* ilog, double* tile_logsum, uint32_t mode) {
+  if (n_inst == 0 || n_blocks == 0) return cudaSuccess;
   if (mode == DM_LOGSUM)
     k_m2_density<true><<<n_blocks, M2_TB, 0, st>>>(ms, n_inst, blk_base, ilog, tile_logsum,
                                                    mode);

@@ -59,6 +59,10 @@ typedef struct {
   float total_ms;           /* device time of the whole call */
   uint64_t candidate_pairs_by_dim[3]; /* same, split by density dimension */
   float pair_kernel_ms_by_dim[3];     /* device time of each persistent launch */
+  float moment_target_ms; /* 2-D strip moments: device time of the target kernel
+                             (k_m2_density), 0 when the call had none */
+  float moment_edge_ms;   /* ... and of the symmetric pair kernel that sums
+                             their edge strips (with any other 2-D pairs) */
 } ent_call_stats;
 
 /* Tile shapes of the pair kernel (0 = keep the current value). */
