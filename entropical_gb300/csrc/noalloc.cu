@@ -18,7 +18,12 @@
 //
 // The device address of the array is looked up once per device, by the
 // first call made with that device current (cudaGetSymbolAddress), and
-// cached; that first call should come before any stream capture.
+// cached; that first call should come before any stream capture. With CUDA's
+// lazy module loading (the default) that first call also loads this
+// library's device code and the array onto the device, so a service that
+// must not allocate after start-up should make one warm-up call then. Every
+// call is synchronous: it copies a few small tables from its own stack and
+// waits for its work on the stream before it returns.
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -83,6 +88,13 @@ int scratch_address(int dev, unsigned char** out) {
   return ENT_OK;
 }
 
+// A failed CUDA call: clear the error state so it does not surface in the
+// caller's next check, and report ENT_ERR_CUDA.
+int cuda_error() {
+  cudaGetLastError();
+  return ENT_ERR_CUDA;
+}
+
 }  // namespace
 
 extern "C" int ent_density_1d_noalloc(const float* d_x, size_t n, float h, double* d_out,
@@ -100,10 +112,8 @@ extern "C" int ent_density_1d_noalloc(const float* d_x, size_t n, float h, doubl
   int rs = scratch_address(dev, &S);
   if (rs) return rs;
   int n_sms = 1;
-  if (cudaDeviceGetAttribute(&n_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
-    cudaGetLastError();
-    return ENT_ERR_CUDA;
-  }
+  if (cudaDeviceGetAttribute(&n_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return cuda_error();
   const uint32_t nn = (uint32_t)n;
   uint32_t* keys = reinterpret_cast<uint32_t*>(S + O_KEYS);
   uint32_t* vals = reinterpret_cast<uint32_t*>(S + O_VALS);
@@ -135,24 +145,22 @@ extern "C" int ent_density_1d_noalloc(const float* d_x, size_t n, float h, doubl
     e = cudaMemcpyAsync(S + O_BLKSEG, blk_seg, 4ull * nb, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(S + O_VIEW, &view, sizeof(view), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(S + O_VIEWOFF, &view_off, 8, cudaMemcpyHostToDevice, st);
-  if (e != cudaSuccess) return ENT_ERR_CUDA;
+  if (e != cudaSuccess) return cuda_error();
 
   // Column statistics: non-finite input and the range for the exact scale.
   const ViewDev* dview = reinterpret_cast<const ViewDev*>(S + O_VIEW);
   ViewStats* dstats = reinterpret_cast<ViewStats*>(S + O_STATS);
-  if (launch_colstats(st, dview, 1, dstats) != cudaSuccess) return ENT_ERR_CUDA;
+  if (launch_colstats(st, dview, 1, dstats) != cudaSuccess) return cuda_error();
   ViewStats vs;
   if (cudaMemcpyAsync(&vs, dstats, sizeof(vs), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-      cudaStreamSynchronize(st) != cudaSuccess) {
-    cudaGetLastError();
-    return ENT_ERR_CUDA;
-  }
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return cuda_error();
   if (vs.nonfinite) return ENT_ERR_NONFINITE;
 
   // Value sort (stable radix sort of orderable keys), in the scratch array.
   if (launch_view_keys(st, dview, reinterpret_cast<const uint64_t*>(S + O_VIEWOFF), 1, nn, keys,
                        vals) != cudaSuccess)
-    return ENT_ERR_CUDA;
+    return cuda_error();
   SegTableDev t;
   t.seg_off = reinterpret_cast<const uint64_t*>(S + O_SEGOFF);
   t.seg_len = reinterpret_cast<const uint32_t*>(S + O_SEGLEN);
@@ -160,7 +168,7 @@ extern "C" int ent_density_1d_noalloc(const float* d_x, size_t n, float h, doubl
   t.blk_seg = reinterpret_cast<const uint32_t*>(S + O_BLKSEG);
   t.hist = reinterpret_cast<uint32_t*>(S + O_HIST);
   if (seg_radix_sort(st, t, 1, nb, keys, vals, keys2, vals2, 0, 32) != cudaSuccess)
-    return ENT_ERR_CUDA;
+    return cuda_error();
 
   // One 1-D instance: exact power-of-two scale, one strip, tiles of TT.
   InstDev I;
@@ -171,7 +179,9 @@ extern "C" int ent_density_1d_noalloc(const float* d_x, size_t n, float h, doubl
   I.S = 1;
   I.n_strips = 1;
   I.ncell1 = I.ncell2 = 1;
-  int k = -std::ilogb(h);
+  // g = h 2^k in [0.5, 1), as the library's other entry points scale it
+  // (the saturating pair bodies need g^2 < 1; this one uses the min-based body)
+  int k = -std::ilogb(h) - 1;
   const double amax = std::fmax(std::fabs((double)vs.mn), std::fabs((double)vs.mx));
   while (k > -126 && amax * std::ldexp(1.0, k) > 1e37) --k;
   k = k < -126 ? -126 : (k > 126 ? 126 : k);
@@ -193,24 +203,22 @@ extern "C" int ent_density_1d_noalloc(const float* d_x, size_t n, float h, doubl
   InstDev* dinst = reinterpret_cast<InstDev*>(S + O_INST);
   if (cudaMemcpyAsync(dinst, &I, sizeof(I), cudaMemcpyHostToDevice, st) != cudaSuccess ||
       cudaMemcpyAsync(S + O_BASE, &base0, 4, cudaMemcpyHostToDevice, st) != cudaSuccess)
-    return ENT_ERR_CUDA;
+    return cuda_error();
   TileDesc* tiles = reinterpret_cast<TileDesc*>(S + O_TILES);
   if (launch_strip_bounds(st, dinst, 1, nn) != cudaSuccess ||
       launch_tile_offsets(st, dinst, 1) != cudaSuccess ||
       launch_gather_pts(st, dinst, 1, nn) != cudaSuccess ||
       launch_plan(st, dinst, 1, reinterpret_cast<const uint32_t*>(S + O_BASE), tiles, I.tile_cap,
                   nsrc) != cudaSuccess)
-    return ENT_ERR_CUDA;
+    return cuda_error();
   int launched = 0;
   if (launch_density(st, 1, (int)R1, tiles, I.tile_cap, dinst, work, err, nullptr, DM_WRITE_F64,
                      n_sms, &launched) != cudaSuccess)
-    return ENT_ERR_CUDA;
+    return cuda_error();
   uint32_t herr = 0;
   if (cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-      cudaStreamSynchronize(st) != cudaSuccess) {
-    cudaGetLastError();
-    return ENT_ERR_CUDA;
-  }
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return cuda_error();
   if (herr & EF_TIMEOUT) return ENT_ERR_TIMEOUT;
   return ENT_OK;
 }
