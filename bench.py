@@ -472,8 +472,18 @@ def other_configs(ctx):
     from oracle import oracle as O
     f1 = O.density_fp64(x1, [0.1])
     _, t_cpu1 = timed_port(lambda: O.density_ref_f32(x1, [0.1], linear_scan=True))
+    # 1-D range sums: the point read by the prefix, target and finish kernels
+    # (3 x 4 B), its 32 B prefix row written and read (2 x 32 B), the sort
+    # (4 passes x 16 B) and the FP64 output (8 B), over the pair-kernel time
+    peak_hbm, _ = hbm_peak_gbs()
+    b1 = (3 * 4 + 2 * 32 + 4 * 16 + 8) * x1.shape[1]
     out["gmm1d_20k"] = {"ms": st.total_ms, "support_pairs": sup,
                         "pairs_per_s": sup / (st.total_ms / 1e3),
+                        "roofline": {"bound": "hbm", "bytes": b1, "achieved_gbs":
+                                     b1 / (st.total_ms / 1e3) / 1e9,
+                                     "frac": b1 / (st.total_ms / 1e3) / 1e9 / peak_hbm,
+                                     "note": "20k points stay in L2; the call is bound by its "
+                                             "launch sequence (about 20 kernels), not by HBM"},
                         "max_rel_err_density_vs_fp64": float(np.max(np.abs(p1 - f1) / f1)),
                         "max_abs_err_vs_fp64": abs(float(-np.mean(np.log(p1)))
                                                    - float(-np.mean(np.log(f1)))),
@@ -509,6 +519,7 @@ def other_configs(ctx):
         "h2d_bytes": int(xt.nbytes),
         "max_abs_err_vs_fp64": te_err, "fp64_oracle_entries": 4, "fp64_oracle_s": t_fp64,
         "roofline_3d": roofline_3d(st.candidate_pairs_by_dim[2], st.pair_kernel_ms_by_dim[2]),
+        "moment_target_ms": st.moment_target_ms, "moment_edge_ms": st.moment_edge_ms,
         "cpu_baseline": {"s": t_cpu3, "pairs_per_s": sup_s3 / t_cpu3,
                          "sample": "3-D density (x5[t+5], x5[t], x17[t]) at 200k frames",
                          "extrapolated_3d_s": sup3 / (sup_s3 / t_cpu3), "kind": "port"}}
@@ -549,7 +560,20 @@ def other_configs(ctx):
         O.density_ref_f32(*ub[q], linear_scan=True)
     t_cpuu = time.perf_counter() - t0
     sup_su = float(sum(O.support_count_fp64(*ub[q]) for q in samp))
+    import torch
+    fpeak, _ = fp32_peak_tflops(torch.cuda.get_device_properties(0).multi_processor_count)
+    # flops per candidate pair of the chosen bodies: symmetric 12 (2-D) / 14
+    # (3-D) per unordered pair, ordered 5 d; range sums and moments have none
+    fl_u = {}
+    for d in (1, 2, 3):
+        v = utuned[f"d{d}"]["pair_variant"]
+        f = {1: 12.0, 2: 12.0, 3: 14.0}[d] if v in (4, 5) else (5.0 * d if v <= 3 else 0.0)
+        ms_d = st.pair_kernel_ms_by_dim[d - 1]
+        tf = f * st.candidate_pairs_by_dim[d - 1] / (ms_d / 1e3) / 1e12 if f and ms_d else None
+        fl_u[f"d{d}"] = {"pair_variant": v, "flops_per_pair": f, "tflops": tf,
+                         "frac": tf / fpeak if tf else None}
     out["uneven_512"] = {"batched_ms": st.total_ms, "sequential_plain_s": seq, "autotuned": utuned,
+                         "roofline_by_dim": fl_u,
                          "max_abs_err_vs_fp64": u_err, "fp64_oracle_instances": 6,
                          "fp64_oracle_s": t_fp64u,
                          "cpu_baseline": {"s": t_cpuu, "pairs_per_s": sup_su / t_cpuu,
