@@ -158,11 +158,11 @@ constexpr int PAIR_MOMENT = 7;
 constexpr uint64_t MOMENT_MIN_POINTS = 1000000;  // default rule: see Ctx::moment_auto
 // Default rule per instance: the moments take a 2-D instance with at least
 // this many in-support neighbours per target (sampled estimate, within 15 %
-// of the true mean on the bench data). Measured: they win 1.5-5x at 19-23k
-// (MI, lagged TE pairs), about break even at 8.5k (joint TE pairs: 5 %
-// faster in the 32-coordinate batch, 10 % slower in an 8-coordinate one) and
-// lose 25 % at 3k (the uneven batch).
-constexpr float MOMENT_MIN_SUPPORT = 6000.f;
+// of the true mean on the bench data). Measured with the edge strips on the
+// symmetric kernel and the fixed-point epilogue (thresholds 0 / 2,000 /
+// 4,000 / 6,000): TE 32 x 200k x 3 lags 1018 / 1021 / 1024 / 1058 ms, the
+// uneven batch's 2-D part 7.64 / 6.86 / 7.07 / 7.30 ms, MI unchanged.
+constexpr float MOMENT_MIN_SUPPORT = 2000.f;
 __host__ __device__ constexpr bool pair_uses_acc(int v) {
   return pair_is_sym(v) || v == PAIR_RANGE || v == PAIR_MOMENT;
 }
