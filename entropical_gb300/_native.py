@@ -70,6 +70,10 @@ SIGNATURES: dict[str, tuple] = {
     "ent_densities_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, c_u32_p,
                                        c_f32_p, c_u32_p, C.c_uint32, C.c_uint32, C.c_void_p,
                                        c_size_p]),
+    "ent_densities_part_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t,
+                                            c_u32_p, c_f32_p, c_u32_p, C.c_uint32, C.c_uint32,
+                                            C.c_uint32, C.c_uint32, C.c_void_p, c_size_p,
+                                            c_f64_p]),
     "ent_support_counts": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, c_u32_p,
                                      c_f32_p, c_u32_p, C.c_uint32, C.c_void_p, c_size_p]),
     "ent_mi_all_pairs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, c_f32_p,

@@ -306,10 +306,13 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
   // pair body per dimension; the symmetric body has no counting mode
   int var_d[4] = {0, 0, 0, 0};
   bool sym_d[4] = {false, false, false, false};
+  bool share = false;  // an instance computes a share of its targets only
+  for (uint32_t i = 0; i < ni; ++i) share = share || insts[i].n_parts > 1;
   for (int d = 1; d <= 3; ++d) {
     int v = c.pair_variant[d - 1];
     if (!density_variant_supported(d, c.tile_r[d - 1], v)) v = 0;
-    if (pair_uses_acc(v) && (mode & DM_COUNT)) v = 2;
+    if (pair_uses_acc(v) && ((mode & DM_COUNT) || share)) v = 2;
+    if (v == 2 && !density_variant_supported(d, c.tile_r[d - 1], v)) v = 0;
     var_d[d] = v;
   }
   // 2-D under PAIR_MOMENT: which instances the strip moments take. Chosen
@@ -383,6 +386,9 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
       std::memset(&I, 0, sizeof(I));
       I.n = s.n;
       I.d = s.d;
+      const uint32_t np = std::max(s.n_parts, 1u);
+      I.t_lo = (uint32_t)((uint64_t)s.n * std::min(s.part, np) / np);
+      I.t_hi = (uint32_t)((uint64_t)s.n * std::min(s.part + 1, np) / np);
       max_n = std::max(max_n, s.n);
       double prod_hg2 = 1.0;
       for (uint32_t j = 0; j < s.d; ++j) {
@@ -1042,7 +1048,8 @@ static int densities_impl(ent_ctx* ctx, const float* coords, size_t n_rows,
                           size_t n_cols, const uint32_t* i_cols, const float* h,
                           const uint32_t* tau, uint32_t d, uint32_t flags,
                           double* out, size_t* n_out, bool device_io,
-                          bool counts) {
+                          bool counts, uint32_t part = 0, uint32_t n_parts = 1,
+                          double* logsum_out = nullptr) {
   if (!ctx) return ENT_ERR_ARG;
   Ctx& c = *reinterpret_cast<Ctx*>(ctx);
   int s = c.begin_call();
@@ -1083,9 +1090,19 @@ static int densities_impl(ent_ctx* ctx, const float* coords, size_t n_rows,
   I.norm = counts ? 1.0 : ((flags & ENT_COMPAT_NORM) ? (double)n_rows : (double)n_sel);
   I.out = dout;
   I.S = c.strip_subdiv;
+  I.part = part;
+  I.n_parts = n_parts;
   Engine eng;
-  s = eng.run(c, views, insts, DM_WRITE_F64 | (counts ? DM_COUNT : 0u), nullptr);
+  EngineOut eo;
+  const bool want_ls = logsum_out && !counts;
+  s = eng.run(c, views, insts, DM_WRITE_F64 | (counts ? DM_COUNT : 0u) | (want_ls ? DM_LOGSUM : 0u),
+              want_ls ? &eo : nullptr);
   if (s) return s;
+  if (want_ls) {
+    e = cudaMemcpyAsync(logsum_out, eo.d_logsum_sorted, sizeof(double), cudaMemcpyDeviceToHost,
+                        c.stream);
+    if (e != cudaSuccess) return c.cuda_fail(e, "copy log-sum");
+  }
   if (!device_io) {
     e = cudaMemcpyAsync(out, dout, 8 * n_sel, cudaMemcpyDeviceToHost, c.stream);
     if (e != cudaSuccess) return c.cuda_fail(e, "copy densities");
@@ -1111,6 +1128,20 @@ int ent_densities_device(ent_ctx* ctx, const float* d_coords, size_t n_rows,
                          double* d_out, size_t* n_out) {
   return densities_impl(ctx, d_coords, n_rows, n_cols, i_cols, h, tau, d, flags,
                         d_out, n_out, true, false);
+}
+
+int ent_densities_part_device(ent_ctx* ctx, const float* d_coords, size_t n_rows,
+                              size_t n_cols, const uint32_t* i_cols, const float* h,
+                              const uint32_t* tau, uint32_t d, uint32_t flags, uint32_t part,
+                              uint32_t n_parts, double* d_out, size_t* n_out,
+                              double* logsum_out) {
+  if (!ctx) return ENT_ERR_ARG;
+  if (n_parts == 0 || part >= n_parts) {
+    Ctx& c = *reinterpret_cast<Ctx*>(ctx);
+    return c.fail(ENT_ERR_ARG, "share index out of range");
+  }
+  return densities_impl(ctx, d_coords, n_rows, n_cols, i_cols, h, tau, d, flags, d_out, n_out,
+                        true, false, part, n_parts, logsum_out);
 }
 
 int ent_support_counts(ent_ctx* ctx, const float* coords, size_t n_rows,

@@ -103,6 +103,11 @@ struct InstSpec {
   uint32_t S = 2;
   // d = 3: cells per bandwidth along dimensions 1 and 2 (0: the context's)
   uint32_t S3[2] = {0, 0};
+  // target share: only the targets at sorted positions [n part / n_parts,
+  // n (part + 1) / n_parts) are computed (the reference's split of one
+  // density's target rows over GPUs); a share runs the ordered pair kernel,
+  // which sums each target fully within its own tile
+  uint32_t part = 0, n_parts = 1;
 };
 
 namespace ent { struct ViewStats; }

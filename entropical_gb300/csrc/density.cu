@@ -264,8 +264,15 @@ __global__ void k_plan(const InstDev* __restrict__ insts, uint32_t n_inst,
   }
   const uint32_t s = a;
   const int d = (int)I.d;
-  const uint32_t tb = I.strip_start[s] + (t - I.tile_off[s]) * I.tt;
-  const uint32_t tc = min(I.tt, I.strip_start[s + 1] - tb);
+  // the tile's targets, clipped to the instance's share [t_lo, t_hi)
+  const uint32_t tb0 = I.strip_start[s] + (t - I.tile_off[s]) * I.tt;
+  const uint32_t te0 = min(tb0 + I.tt, I.strip_start[s + 1]);
+  const uint32_t tb = max(tb0, I.t_lo), te = min(te0, I.t_hi);
+  if (te <= tb) {  // outside the share
+    tiles[g] = td;
+    return;
+  }
+  const uint32_t tc = te - tb;
   const float yf = y0_at(I.pts, d, tb);
   const float yl = y0_at(I.pts, d, tb + tc - 1);
   // half-width g0 = sqrt(g0^2), widened so that rounding can only add

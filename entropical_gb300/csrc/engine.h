@@ -76,6 +76,7 @@ struct InstDev {
                             // above), the symmetric pair kernel sums those
                             // pairs into acc and its finish skips it
   uint32_t pad2;
+  uint32_t t_lo, t_hi;      // targets computed: sorted positions [t_lo, t_hi)
 };
 
 struct TileDesc {

@@ -196,6 +196,8 @@ extern "C" int ent_density_1d_noalloc(const float* d_x, size_t n, float h, doubl
   I.tile_off = reinterpret_cast<uint32_t*>(S + O_TILEOFF);
   I.tt = TT;
   I.tile_cap = (nn + TT - 1) / TT + 1;
+  I.t_lo = 0;  // every target
+  I.t_hi = nn;
   I.tile_base = 0;
   I.scale = 0.75 / ((double)nn * (double)h * (double)I.g2[0]);
   I.out = d_out;

@@ -215,6 +215,26 @@ class Context:
         self.check(st)
         return n_out.value
 
+    def combined_densities_part_device(self, d_coords: int, n_rows: int, n_cols: int,
+                                       i_cols: Sequence[int], h: Sequence[float],
+                                       tau: Sequence[int] | None, part: int, n_parts: int,
+                                       d_out: int, compat_norm: bool = False
+                                       ) -> tuple[int, float]:
+        """One share of one density's targets (of n_parts, in the library's
+        sorted order) against every source: their densities into d_out (device,
+        by original index; other entries untouched). Returns (n_sel, sum of
+        log p over the share's targets)."""
+        d, cols, hv, tv = self._selection(i_cols, h, tau)
+        n_out = C.c_size_t(0)
+        ls = C.c_double(0.0)
+        st = self._lib.ent_densities_part_device(
+            self._h, C.c_void_p(d_coords), n_rows, n_cols, cols.ctypes.data_as(c_u32_p),
+            hv.ctypes.data_as(c_f32_p), tv.ctypes.data_as(c_u32_p) if tv is not None else None,
+            d, COMPAT_NORM if compat_norm else 0, int(part), int(n_parts), C.c_void_p(d_out),
+            C.byref(n_out), C.byref(ls))
+        self.check(st)
+        return n_out.value, ls.value
+
     def support_counts(self, coords, n_rows: int | None, i_cols: Sequence[int],
                        h: Sequence[float], tau: Sequence[int] | None = None) -> np.ndarray:
         """Per point, the number of sources inside the product-kernel support."""

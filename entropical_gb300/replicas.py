@@ -2,7 +2,7 @@
 
 The density path splits into independent objects (densities, hence MI pairs,
 TE (pair, lag) entries, trajectories), so N GPUs never exchange data on the
-path. Two forms:
+path. Three forms:
 
 * weak scaling (bench.py under torchrun): every rank computes its own
   problem of the benchmark's size (rank r: the benchmark data with seed +r);
@@ -14,12 +14,15 @@ path. Two forms:
   batch (``Context.mi_entropies_device`` / ``te_entropies_device``: only the
   views its share uses are sorted), and the entropies -- a few KB -- are
   gathered on the host to assemble the MI matrix or the TE tensor. Shares are
-  dealt by an estimate of each density's cost (``WEIGHTS``), not by count.
+  dealt by an estimate of each density's cost (``WEIGHTS``), not by count;
+* one density split over ranks (``densities_split``), as the reference's
+  per-GPU driver splits its target rows (density_1d.cuh:181-219): every rank
+  computes one share of the targets against every source
+  (``Context.combined_densities_part_device``) into a zeroed buffer, and the
+  shares are added on the host (each target is written by one rank only).
 
-The reference splits one density's target rows over its GPUs instead
-(density_1d.cuh:181-219); dealing whole densities needs no host reduction of
-partial sums. Only the report and the final scalars cross ranks; no
-collective is on the data path.
+Only the report, the final scalars or the per-point densities of a split
+density cross ranks; no collective is on the data path.
 """
 from __future__ import annotations
 
@@ -174,3 +177,27 @@ def te_all_pairs_split(ctx, d_coords: int, n_rows: int, n_cols: int, h: Sequence
     H = split_entropies(
         lambda items: ctx.te_entropies_device(d_coords, n_rows, n_cols, h, taus, items), w, dist)
     return te_assemble(n_cols, len(taus), H)
+
+
+def densities_split(ctx, d_coords: int, n_rows: int, n_cols: int, i_cols: Sequence[int],
+                    h: Sequence[float], tau: Sequence[int] | None = None,
+                    dist=None, device=None) -> tuple[np.ndarray, float]:
+    """One density of the device matrix d_coords with its targets split over
+    the ranks of dist: rank r computes share r into a zeroed buffer on
+    ``device`` (default: the current CUDA device), the shares are summed on
+    the host. Returns (densities by original index, entropy -mean log p), the
+    same on every rank."""
+    import torch
+    rank, world = _world(dist)
+    n_sel = n_rows - (max(tau) if tau else 0)
+    dev = device if device is not None else torch.cuda.current_device()
+    buf = torch.zeros(n_sel, dtype=torch.float64, device=dev)
+    _, ls = ctx.combined_densities_part_device(d_coords, n_rows, n_cols, i_cols, h, tau, rank,
+                                               world, buf.data_ptr())
+    p = buf.cpu().numpy()
+    if world > 1:
+        parts = [None] * world
+        dist.all_gather_object(parts, (p, ls))
+        p = np.sum([q for q, _ in parts], axis=0)
+        ls = float(sum(v for _, v in parts))
+    return p, -ls / n_sel

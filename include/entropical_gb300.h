@@ -154,6 +154,24 @@ int ent_densities_device(ent_ctx* ctx, const float* d_coords, size_t n_rows,
                          size_t n_cols, const uint32_t* i_cols, const float* h,
                          const uint32_t* tau, uint32_t d, uint32_t flags,
                          double* d_out, size_t* n_out);
+/*
+ * One share of one density's targets, for splitting a single large density
+ * over GPUs as the reference's per-GPU driver splits its target rows
+ * (density_1d.cuh:181-219, host reduction :94-104): of the n_sel targets,
+ * in the library's sorted order, this call computes those at positions
+ * [n_sel part / n_parts, n_sel (part + 1) / n_parts) against every source and
+ * writes their densities to d_out (device, n_sel doubles, indexed by
+ * original point); the other entries of d_out are left untouched, so shares
+ * computed into zeroed buffers add up to the whole. logsum_out (nullable, on
+ * the host) receives the sum of log p over the share's targets. Each share
+ * runs the ordered pair kernel (every target summed fully in its own tile).
+ * Same arguments and normalisation as ent_densities_device otherwise.
+ */
+int ent_densities_part_device(ent_ctx* ctx, const float* d_coords, size_t n_rows,
+                              size_t n_cols, const uint32_t* i_cols, const float* h,
+                              const uint32_t* tau, uint32_t d, uint32_t flags, uint32_t part,
+                              uint32_t n_parts, double* d_out, size_t* n_out,
+                              double* logsum_out);
 
 /*
  * Number of (target, source) pairs inside the kernel support for the same

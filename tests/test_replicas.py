@@ -9,8 +9,9 @@ import pytest
 
 import numpy as np
 
-from entropical_gb300.replicas import (WEIGHTS, aggregate, deal, mi_assemble, mi_instances, shard,
-                                       split_entropies, te_assemble, te_instances)
+from entropical_gb300.replicas import (WEIGHTS, aggregate, deal, densities_split, mi_assemble,
+                                       mi_instances, shard, split_entropies, te_assemble,
+                                       te_instances)
 
 
 def _free_port():
@@ -131,3 +132,50 @@ def test_te_assemble_formula():
                 ref = (H[idx[(q, 3, a, b)]] + H[idx[(q, 2, i, i)]] - H[idx[(q, 4, i, j)]]
                        - H[idx[(q, 1, i, i)]])
                 assert te[q, i, j] == ref
+
+
+class _FakeShareContext:
+    """Stands in for the GPU call: writes share `part` of a fixed density
+    vector through the pointer it is given (host memory here)."""
+    def __init__(self, p):
+        self.p = p
+
+    def combined_densities_part_device(self, d_coords, n_rows, n_cols, i_cols, h, tau, part,
+                                       n_parts, d_out):
+        import ctypes as C
+        n = len(self.p)
+        lo, hi = n * part // n_parts, n * (part + 1) // n_parts
+        out = np.ctypeslib.as_array((C.c_double * n).from_address(d_out))
+        out[lo:hi] = self.p[lo:hi]
+        return n, float(np.sum(np.log(self.p[lo:hi])))
+
+
+def _dens_worker(rank, world, port, out):
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    p = np.random.default_rng(6).uniform(0.1, 2.0, 1001)
+    dens, H = densities_split(_FakeShareContext(p), 0, 1001, 1, [0], [0.3], None, dist,
+                              device="cpu")
+    out.put((rank, dens.tolist(), H))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_density_split_over_two_gloo_ranks():
+    mp = pytest.importorskip("torch.multiprocessing")
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_dens_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    ref = np.random.default_rng(6).uniform(0.1, 2.0, 1001)
+    for _, dens, H in res:
+        assert np.array_equal(np.array(dens), ref)
+        assert abs(H - (-np.mean(np.log(ref)))) < 1e-12
