@@ -398,7 +398,7 @@ def compare_plain(ctx, pctx, x, ptr, log_fp64_pairs=2):
     return out
 
 
-def compare_plain_te(ctx, pctx, n_coords=8, taus=(1, 5, 10)):
+def compare_plain_te(ctx, pctx, n_coords=32, taus=(1, 5, 10)):
     """Transfer entropy of all ordered pairs over the first n_coords of the
     coupled-Langevin data (200k frames, 3 lags), bandwidths by the AMISE
     search, two ways: plain -- per column 16 epa_convolution calls driven by
@@ -445,12 +445,17 @@ def compare_plain_te(ctx, pctx, n_coords=8, taus=(1, 5, 10)):
     sync()
     t0 = time.perf_counter()
     hl, st = learned.hestimate_learned(ctx, net, list(x), skip_levels=6)
+    t_h = time.perf_counter() - t0
     te_b = ctx.te_all_pairs(x, hl[:, 0], list(taus))
     t_b = time.perf_counter() - t0
+    cs = ctx.last_stats()
     off = ~np.eye(M, dtype=bool)
     return {"workload": f"AMISE bandwidths for {M} columns, then TE of all {M * (M - 1)} ordered "
                         f"pairs at lags {list(taus)} ({M} x {N} Langevin)",
             "plain_s": t_plain, "plain_density_calls": calls, "batched_learned_s": t_b,
+            "learned_hestimate_s": t_h, "batched_te_device_ms": cs.total_ms,
+            "batched_te_pair_kernel_ms_by_dim": list(cs.pair_kernel_ms_by_dim),
+            "h_over_scott_median": float(np.median(hl[:, 0] / workloads.scott_bandwidth(x, 3))),
             "speedup": t_plain / t_b, "te_estimates": int(len(taus) * M * (M - 1)),
             "bandwidths_identical": bool(np.array_equal(hl[:, 0], hp)),
             "max_abs_dTE_batched_vs_plain": float(np.max(np.abs(te_b - te_plain)[:, off])),

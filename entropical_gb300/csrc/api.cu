@@ -55,7 +55,7 @@ void* Arena::alloc(size_t bytes) {
   return p;
 }
 
-void Arena::reset() {
+void Arena::coalesce() {
   if (blocks.size() > 1) {
     size_t want = std::max(total_used, (size_t)64 << 20);
     for (auto& b : blocks) cudaFree(b.ptr);
@@ -64,6 +64,10 @@ void Arena::reset() {
     if (cudaMalloc(&p, want) == cudaSuccess) blocks.push_back({p, want});
     else cudaGetLastError();
   }
+}
+
+void Arena::reset() {
+  coalesce();
   used_in_last = 0;
   total_used = 0;
 }
@@ -109,6 +113,9 @@ int Ctx::end_call() {
   cudaEventRecord(ev_call1, stream);
   cudaError_t e = cudaStreamSynchronize(stream);
   if (e != cudaSuccess) return cuda_fail(e, "kernel execution");
+  // A call that outgrew the workspace left it in several blocks; join them
+  // now, while the work is done, so the next call starts from one block.
+  arena.coalesce();
   uint32_t err = 0;
   e = cudaMemcpy(&err, d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_fail(e, "read error word");

@@ -12,8 +12,8 @@
 
 namespace ent { struct ILogEntry; }
 
-// Grow-only device workspace. Blocks are kept across calls; when a call
-// needed more than one block, the next call coalesces them into one.
+// Grow-only device workspace. Blocks are kept across calls; a call that
+// needed more than one block coalesces them into one when it ends.
 struct Arena {
   struct Block {
     void* ptr;
@@ -24,6 +24,7 @@ struct Arena {
   size_t total_used = 0;
   void* alloc(size_t bytes);
   void reset();
+  void coalesce();  // one block of the current use's size (contents discarded)
   void release();
   size_t spare() const;  // bytes left in the blocks already held
 };
