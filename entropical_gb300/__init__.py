@@ -9,7 +9,8 @@ built on them. There is no CPU implementation of any of these here.
 from ._build import build, lib_path  # noqa: F401
 from ._native import NativeError  # noqa: F401
 from .densities import (COMPAT_NORM, Context, as_colmajor, combined_densities,  # noqa: F401
-                        coords_file_shape, default_context, read_coords)
+                        coords_file_shape, default_context, is_xtc, read_coords, write_xtc,
+                        xtc_file_shape)
 
 __all__ = [
     "build",
@@ -21,5 +22,8 @@ __all__ = [
     "combined_densities",
     "coords_file_shape",
     "read_coords",
+    "is_xtc",
+    "xtc_file_shape",
+    "write_xtc",
     "default_context",
 ]

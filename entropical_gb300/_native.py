@@ -99,6 +99,14 @@ SIGNATURES: dict[str, tuple] = {
     "ent_load_coords_device": (C.c_int, [C.c_void_p, C.c_char_p, c_size_p, C.c_size_t,
                                          C.c_void_p, C.c_size_t, C.c_size_t]),
     "ent_io_last_error": (C.c_char_p, []),
+    "ent_xtc_file_shape": (C.c_int, [C.c_char_p, c_size_p, c_size_p]),
+    "ent_load_xtc_device": (C.c_int, [C.c_void_p, C.c_char_p, c_size_p, C.c_size_t,
+                                      C.c_void_p, C.c_size_t, C.c_size_t]),
+    "ent_read_xtc": (C.c_int, [C.c_void_p, C.c_char_p, c_size_p, C.c_size_t, C.c_char,
+                               C.c_void_p, C.c_size_t, C.c_size_t]),
+    "ent_write_xtc": (C.c_int, [C.c_char_p, C.c_void_p, C.c_size_t, C.c_size_t, C.c_char,
+                                C.c_float]),
+    "ent_xtc_last_error": (C.c_char_p, []),
     "ent_te_all_pairs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, c_f32_p,
                                    c_u32_p, C.c_size_t, C.c_uint32, c_f64_p]),
     "ent_te_all_pairs_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t,

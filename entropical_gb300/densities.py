@@ -62,8 +62,51 @@ def _io_check(st: int) -> None:
                           lib.ent_status_string(st).decode())
 
 
+def is_xtc(path) -> bool:
+    """True for names CoordsFile::open gives to its XTC handler: longer than
+    four characters and ending in ".xtc" (coords_file.cpp:137-145)."""
+    name = os.fsdecode(path)
+    return len(name) > 4 and name.endswith(".xtc")
+
+
+def _xtc_check(st: int) -> None:
+    if st != 0:
+        lib = _native.load()
+        raise NativeError(st, (lib.ent_xtc_last_error() or b"").decode() or
+                          lib.ent_status_string(st).decode())
+
+
+def xtc_file_shape(path) -> tuple[int, int]:
+    """(frames, 3 natoms) of an XTC trajectory."""
+    lib = _native.load()
+    r, c = C.c_size_t(), C.c_size_t()
+    _xtc_check(lib.ent_xtc_file_shape(os.fsencode(path), C.byref(r), C.byref(c)))
+    return r.value, c.value
+
+
+def write_xtc(path, coords, precision: float = 1000.0, primary: str = "C") -> None:
+    """Write coordinates as XTC frames, one per row, as XtcHandler::write does
+    (coords_file.cpp:112-126): step and time = row, zero box, precision 1000
+    unless given. primary 'C': coords is (n_cols, n_rows), one row per
+    coordinate like the other calls take; 'R': (n_rows, n_cols), one row per
+    frame. n_cols = 3 natoms (x, y, z per atom). Encoded by all host threads;
+    the bytes equal the reference's writer's."""
+    if primary not in ("C", "R"):
+        raise ValueError("primary must be 'C' or 'R'")
+    a = np.ascontiguousarray(coords, dtype=np.float32)
+    if a.ndim != 2:
+        raise ValueError("coords must be 2-D")
+    n_rows, n_cols = (a.shape[1], a.shape[0]) if primary == "C" else a.shape
+    lib = _native.load()
+    _xtc_check(lib.ent_write_xtc(os.fsencode(path), a.ctypes.data_as(C.c_void_p), n_rows,
+                                 n_cols, primary.encode(), float(precision)))
+
+
 def coords_file_shape(path) -> tuple[int, int]:
-    """(n_rows, n_cols) of a coordinate file in the reference's ASCII format."""
+    """(n_rows, n_cols) of a coordinate file: the reference's ASCII format,
+    or an XTC trajectory for names ending in ".xtc" (frames, 3 natoms)."""
+    if is_xtc(path):
+        return xtc_file_shape(path)
     lib = _native.load()
     r, c = C.c_size_t(), C.c_size_t()
     _io_check(lib.ent_coords_file_shape(os.fsencode(path), C.byref(r), C.byref(c)))
@@ -491,7 +534,11 @@ class Context:
     def load_coords_device(self, path, d_out: int, usecols=None) -> tuple[int, int]:
         """Parse a coordinate file into the column-major device matrix at
         address d_out (n_rows x n_cols floats; see coords_file_shape), with
-        pinned, overlapped host-to-device copies. Returns (n_rows, n_cols)."""
+        pinned, overlapped host-to-device copies. Names ending in ".xtc" are
+        XTC trajectories, decoded on the device (load_xtc_device), as
+        CoordsFile::open picks its handler. Returns (n_rows, n_cols)."""
+        if is_xtc(path):
+            return self.load_xtc_device(path, d_out, usecols)
         n_rows, n_all = coords_file_shape(path)
         uc = _usecols(usecols)
         n_cols = n_all if uc is None else len(set(int(c) for c in uc))
@@ -500,6 +547,38 @@ class Context:
             0 if uc is None else len(uc), C.c_void_p(d_out), n_rows, n_cols)
         self.check(st)
         return n_rows, n_cols
+
+    def _xtc_shape(self, path, usecols):
+        n_rows, n_all = xtc_file_shape(path)
+        uc = _usecols(usecols)
+        n_cols = n_all if uc is None else len(set(int(c) for c in uc))
+        return n_rows, n_cols, uc
+
+    def load_xtc_device(self, path, d_out: int, usecols=None) -> tuple[int, int]:
+        """Decode an XTC trajectory on the device into the column-major matrix
+        at d_out (frames x columns; column 3a + c is coordinate c of atom a).
+        The compressed file is what is copied to the device. Returns
+        (n_rows, n_cols)."""
+        n_rows, n_cols, uc = self._xtc_shape(path, usecols)
+        st = self._lib.ent_load_xtc_device(
+            self._h, os.fsencode(path), None if uc is None else uc.ctypes.data_as(c_size_p),
+            0 if uc is None else len(uc), C.c_void_p(d_out), n_rows, n_cols)
+        self.check(st)
+        return n_rows, n_cols
+
+    def read_xtc(self, path, usecols=None, primary: str = "C") -> np.ndarray:
+        """XTC trajectory decoded on the device, returned in host memory:
+        primary 'C' as an (n_cols, n_frames) array (one row per coordinate,
+        the layout the other calls take), 'R' as (n_frames, n_cols) (the rows
+        XtcHandler::next returns)."""
+        n_rows, n_cols, uc = self._xtc_shape(path, usecols)
+        out = np.empty((n_cols, n_rows) if primary == "C" else (n_rows, n_cols), np.float32)
+        st = self._lib.ent_read_xtc(
+            self._h, os.fsencode(path), None if uc is None else uc.ctypes.data_as(c_size_p),
+            0 if uc is None else len(uc), primary.encode(), out.ctypes.data_as(C.c_void_p),
+            n_rows, n_cols)
+        self.check(st)
+        return out
 
     # ---------------------------------------------------- neighbour search
     def neighbor_windows(self, col, h: float) -> tuple[np.ndarray, np.ndarray]:

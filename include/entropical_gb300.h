@@ -321,6 +321,38 @@ int ent_load_coords_device(ent_ctx* ctx, const char* path, const size_t* usecols
 /* Message of the last failing file call of this thread (empty if none). */
 const char* ent_io_last_error(void);
 
+/*
+ * XTC trajectories, the format CoordsFile::open picks for names ending in
+ * ".xtc" (coords_file/coords_file.cpp:137-145; XtcHandler :70-126, the
+ * reference's vendored xdrfile codec). A frame is one row of 3 * natoms
+ * values (x0, y0, z0, x1, ...), as XtcHandler::next returns it; reading stops
+ * at the first frame that does not parse, as XtcHandler::next does.
+ */
+/* Frames and columns (3 natoms) of an XTC file (host only). */
+int ent_xtc_file_shape(const char* path, size_t* n_frames, size_t* n_cols);
+/* Decode the file on the device into the column-major n_rows x n_cols_out
+ * matrix d_out (device memory of ctx's device): the file is indexed on the
+ * host, copied to the device through pinned buffers and decoded by one
+ * thread per frame. usecols as for ent_read_coords (the file's column
+ * order). A malformed compressed frame is ENT_ERR_IO naming the frame. */
+int ent_load_xtc_device(ent_ctx* ctx, const char* path, const size_t* usecols,
+                        size_t n_usecols, float* d_out, size_t n_rows, size_t n_cols_out);
+/* Same into host memory: primary_index 'C' column-major, 'R' row-major (the
+ * rows XtcHandler::next returns, one after another). */
+int ent_read_xtc(ent_ctx* ctx, const char* path, const size_t* usecols, size_t n_usecols,
+                 char primary_index, float* out, size_t n_rows, size_t n_cols_out);
+/* Write n_rows frames of n_cols = 3 natoms columns (host memory, 'C' or 'R'
+ * layout) as XtcHandler::write does (coords_file.cpp:112-126): frame r has
+ * step r, time r, a zero box and the given precision (<= 0: 1000, the
+ * handler's). The bytes equal the reference's writer's. Host only; frames are
+ * encoded by all host threads. Coordinates that overflow 32-bit integers at
+ * the precision, or atoms too far apart for the format's table, are
+ * ENT_ERR_ARG (the reference writes a frame it cannot read back). */
+int ent_write_xtc(const char* path, const float* coords, size_t n_rows, size_t n_cols,
+                  char primary_index, float precision);
+/* Message of the last failing host-only XTC call of this thread. */
+const char* ent_xtc_last_error(void);
+
 /* ------------------------------------ the reference's estimator formulas */
 
 #define ENT_BATCH_DEVICE_OUTPUT 8u /* ent_dens_all: out is a device pointer */

@@ -81,6 +81,16 @@ float orc_amise_from_conv(float conv, float h, size_t n);
 float orc_hestimate_amise(const float* col, size_t n, int exact_conv,
                           int* n_conv);
 
+/* XTC trajectories (xtc_oracle.c): the reading side of CoordsFile::
+ * XtcHandler (coords_file/coords_file.cpp:90-110, xdrfile_xtc.c:83-95,
+ * xdrfile.c:761-961). orc_xtc_shape: frames up to the first that does not
+ * parse, and the atom count (0 ok, -1 unreadable, -2 no frame).
+ * orc_read_xtc: frames [f0, f1) into out[(3a + c) * n_out_rows + (f - f0)]
+ * (x, y, z of atom a: columns 3a, 3a+1, 3a+2); returns the frames read, or
+ * -1 (unreadable) / -2 (malformed compressed frame). */
+int orc_xtc_shape(const char* path, size_t* n_frames, size_t* n_atoms);
+long orc_read_xtc(const char* path, size_t f0, size_t f1, float* out, size_t n_out_rows);
+
 #ifdef __cplusplus
 }
 #endif

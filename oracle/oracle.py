@@ -384,3 +384,79 @@ def ref_run_mode(mode: str, coords: np.ndarray, bandwidths, workdir: Path, tau: 
         rows = [ln.split() for ln in fout.read_text().splitlines() if ln.strip()]
         return np.array([float(r[1]) for r in rows])
     return np.loadtxt(fout, ndmin=2)
+
+
+# ------------------------------------------------------------- XTC files
+XDR_SO = HERE / "_ref" / "libentxdr.so"
+_xdr = None
+
+
+def xtc_shape(path) -> tuple[int, int]:
+    """(frames, natoms) by the oracle's XTC reader (xtc_oracle.c)."""
+    lib = orc()
+    nf, na = C.c_size_t(), C.c_size_t()
+    st = lib.orc_xtc_shape(str(path).encode(), C.byref(nf), C.byref(na))
+    if st != 0:
+        raise ValueError(f"orc_xtc_shape: {st}")
+    return nf.value, na.value
+
+
+def read_xtc(path, f0: int = 0, f1: int | None = None) -> np.ndarray:
+    """Frames [f0, f1) as rows of 3 natoms floats, decoded by the oracle's
+    restatement of read_xtc (xtc_oracle.c)."""
+    lib = orc()
+    lib.orc_read_xtc.restype = C.c_long
+    n_frames, natoms = xtc_shape(path)
+    f1 = n_frames if f1 is None else min(f1, n_frames)
+    out = np.zeros((3 * natoms, f1 - f0), np.float32)
+    got = lib.orc_read_xtc(str(path).encode(), C.c_size_t(f0), C.c_size_t(f1), _p(out),
+                           C.c_size_t(f1 - f0))
+    if got != f1 - f0:
+        raise ValueError(f"orc_read_xtc: {got}")
+    return np.ascontiguousarray(out.T)
+
+
+def xdr_available() -> bool:
+    return XDR_SO.exists()
+
+
+def xdr() -> C.CDLL:
+    """The reference's vendored xdrfile, compiled in place (make -C oracle ref)."""
+    global _xdr
+    if _xdr is None:
+        lib = C.CDLL(str(XDR_SO))
+        lib.xdrfile_open.restype = C.c_void_p
+        lib.xdrfile_open.argtypes = [C.c_char_p, C.c_char_p]
+        lib.xdrfile_close.argtypes = [C.c_void_p]
+        lib.write_xtc.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_void_p,
+                                  C.c_void_p, C.c_float]
+        lib.read_xtc.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float),
+                                 C.c_void_p, C.c_void_p, C.POINTER(C.c_float)]
+        _xdr = lib
+    return _xdr
+
+
+def ref_write_xtc(path, rows: np.ndarray, precision: float = 1000.0) -> None:
+    """XtcHandler::write for every row (coords_file.cpp:112-126): step and
+    time = the row, zero box."""
+    lib = xdr()
+    xd = lib.xdrfile_open(str(path).encode(), b"w")
+    box = np.zeros((3, 3), np.float32)
+    for r, row in enumerate(np.asarray(rows, np.float32)):
+        x = np.ascontiguousarray(row.reshape(-1, 3))
+        lib.write_xtc(xd, x.shape[0], r, float(r), _p(box), _p(x), precision)
+    lib.xdrfile_close(xd)
+
+
+def ref_read_xtc(path, natoms: int) -> np.ndarray:
+    """XtcHandler::next until it reports the end (coords_file.cpp:90-110)."""
+    lib = xdr()
+    xd = lib.xdrfile_open(str(path).encode(), b"r")
+    box = np.zeros((3, 3), np.float32)
+    x = np.zeros((natoms, 3), np.float32)
+    step, t, p = C.c_int(), C.c_float(), C.c_float()
+    out = []
+    while lib.read_xtc(xd, natoms, C.byref(step), C.byref(t), _p(box), _p(x), C.byref(p)) == 0:
+        out.append(x.reshape(-1).copy())
+    lib.xdrfile_close(xd)
+    return np.array(out, np.float32).reshape(len(out), 3 * natoms)
