@@ -68,6 +68,10 @@ def parse():
                     help="time only the transfer-entropy batch over the first N coordinates of "
                          "the 32 x 200k Langevin data (lags 1, 5, 10): the small case for ncu "
                          "captures of the 3-D kernel; prints a JSON line of its own")
+    ap.add_argument("--xtc-frames", type=int, default=0,
+                    help="time only the XTC trajectory load (1000 atoms x N frames): the small "
+                         "case for ncu captures of the decode kernel; prints a JSON line of its "
+                         "own")
     ap.add_argument("--coords", type=int, default=N_COORDS,
                     help="coordinates of the MI batch (64 = the benchmark workload; "
                          "smaller values give the small case used for ncu captures)")
@@ -667,7 +671,7 @@ def xtc_config(ctx, n_atoms: int = 1000, n_frames: int = 50_000):
     on a sample."""
     import tempfile
     import torch
-    from entropical_gb300 import write_xtc
+    from entropical_gb300 import write_xtc, xtc_file_shape
     from oracle import oracle as O
     rows = xtc_trajectory(n_atoms, n_frames)
     out = {"workload": f"{n_atoms} atoms x {n_frames} frames ({3 * n_atoms} coordinates), "
@@ -689,6 +693,9 @@ def xtc_config(ctx, n_atoms: int = 1000, n_frames: int = 50_000):
             walls.append(time.perf_counter() - t0)
             kern.append(ctx.last_stats().pair_kernel_ms)
         wall, k_ms = min(walls), float(np.median(kern))
+        t0 = time.perf_counter()
+        xtc_file_shape(path)
+        t_index = time.perf_counter() - t0
         sample = 2000
         got = dev[:, :sample].cpu().numpy()
         t0 = time.perf_counter()
@@ -704,7 +711,7 @@ def xtc_config(ctx, n_atoms: int = 1000, n_frames: int = 50_000):
         "file_bytes": size, "bytes_per_coordinate": size / (3 * n_atoms * n_frames),
         "load_device_s": wall, "load_device_MB_per_s": size / wall / 1e6,
         "coordinates_per_s": 3 * n_atoms * n_frames / wall,
-        "decode_kernel_ms": k_ms,
+        "decode_kernel_ms": k_ms, "index_s": t_index,
         "decode_roofline": {"bound": "latency (one serial bit stream per thread)",
                             "algorithmic_bytes": size + out_bytes,
                             "achieved_gbs": (size + out_bytes) / (k_ms / 1e3) / 1e9,
@@ -804,6 +811,10 @@ def main():
     args = parse()
     if args.te_coords:
         return te_only(args)
+    if args.xtc_frames:
+        from entropical_gb300 import Context
+        print(json.dumps(xtc_config(Context(), n_frames=args.xtc_frames)))
+        return None
     ws, rank, local = dist_env()
     from entropical_gb300 import workloads
     # weak scaling over independent problems: rank r computes the benchmark

@@ -109,6 +109,27 @@ int Ctx::begin_call() {
   return ENT_OK;
 }
 
+int Ctx::ensure_staging(size_t bytes) {
+  if (stage_bytes >= bytes) return ENT_OK;
+  for (int k = 0; k < 2; ++k) {
+    if (h_stage[k]) cudaFreeHost(h_stage[k]);
+    h_stage[k] = nullptr;
+  }
+  stage_bytes = 0;
+  for (int k = 0; k < 2; ++k) {
+    cudaError_t e = cudaHostAlloc(reinterpret_cast<void**>(&h_stage[k]), bytes,
+                                  cudaHostAllocDefault);
+    if (e == cudaSuccess && !ev_stage[k])
+      e = cudaEventCreateWithFlags(&ev_stage[k], cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+      h_stage[k] = nullptr;
+      return cuda_fail(e, "pinned staging");
+    }
+  }
+  stage_bytes = bytes;
+  return ENT_OK;
+}
+
 int Ctx::end_call() {
   cudaEventRecord(ev_call1, stream);
   cudaError_t e = cudaStreamSynchronize(stream);
@@ -907,6 +928,10 @@ void ent_destroy(ent_ctx* ctx) {
   for (int k = 0; k < 2; ++k) {
     cudaEventDestroy(c->ev_m[k][0]);
     cudaEventDestroy(c->ev_m[k][1]);
+  }
+  for (int k = 0; k < 2; ++k) {
+    if (c->h_stage[k]) cudaFreeHost(c->h_stage[k]);
+    if (c->ev_stage[k]) cudaEventDestroy(c->ev_stage[k]);
   }
   cudaStreamDestroy(c->stream);
   delete c;

@@ -77,6 +77,13 @@ struct Ctx {
   // and grids) instead of being instantiated anew.
   cudaGraphExec_t graph_exec = nullptr;
   uint32_t graph_updates = 0, graph_instantiations = 0;
+  // Pinned host staging for file loads: two buffers of stage_bytes, filled
+  // by the host threads in turn while the other one is being copied; kept
+  // across calls (allocated on first use, freed with the context).
+  uint8_t* h_stage[2] = {nullptr, nullptr};
+  cudaEvent_t ev_stage[2] = {nullptr, nullptr};
+  size_t stage_bytes = 0;
+  int ensure_staging(size_t bytes);
 
   // grid of a persistent kernel: resident CTAs per SM x SMs, capped by work
   unsigned persistent_grid(uint32_t n_work, const void* kern, int threads, size_t smem);

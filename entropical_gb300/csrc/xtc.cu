@@ -31,6 +31,7 @@
 // prints a warning and writes a frame it cannot read back).
 #include <cuda_runtime.h>
 #include <fcntl.h>
+#include <sys/mman.h>
 #include <sys/stat.h>
 #include <unistd.h>
 
@@ -119,8 +120,8 @@ bool pread_all(int fd, uint8_t* dst, size_t len, uint64_t off) {
   return true;
 }
 
-// Walks the frame headers (two header reads per frame: the fixed part and,
-// for compressed frames, the byte count).
+// Walks the frame headers through a read-only mapping of the file: one
+// header read per frame, no system call per frame.
 bool index_xtc(const char* path, XtcIndex* ix, std::string* err) {
   Fd f;
   f.fd = open(path, O_RDONLY);
@@ -134,10 +135,18 @@ bool index_xtc(const char* path, XtcIndex* ix, std::string* err) {
     return false;
   }
   const uint64_t size = (uint64_t)st.st_size;
+  const uint8_t* m = nullptr;
+  if (size >= XTC_HEAD) {
+    void* p = mmap(nullptr, (size_t)size, PROT_READ, MAP_PRIVATE, f.fd, 0);
+    if (p == MAP_FAILED) {
+      *err = "cannot map the file";
+      return false;
+    }
+    m = static_cast<const uint8_t*>(p);
+  }
   uint64_t off = 0;
-  uint8_t h[XTC_CHEAD];
-  while (off + XTC_HEAD <= size) {
-    if (!pread_all(f.fd, h, XTC_HEAD, off)) break;
+  while (m && off + XTC_HEAD <= size) {
+    const uint8_t* h = m + off;
     const int32_t magic = (int32_t)be32(h), natoms = (int32_t)be32(h + 4);
     const int32_t lsize = (int32_t)be32(h + 52);
     if (magic != XTC_MAGIC || natoms <= 0 || lsize != natoms) break;
@@ -147,13 +156,14 @@ bool index_xtc(const char* path, XtcIndex* ix, std::string* err) {
     if (natoms <= 9) {
       len = XTC_HEAD + 12ull * (uint64_t)natoms;
     } else {
-      if (off + XTC_CHEAD > size || !pread_all(f.fd, h, 4, off + XTC_CHEAD - 4)) break;
-      len = XTC_CHEAD + (((uint64_t)be32(h) + 3) & ~3ull);
+      if (off + XTC_CHEAD > size) break;
+      len = XTC_CHEAD + (((uint64_t)be32(h + XTC_CHEAD - 4) + 3) & ~3ull);
     }
     if (off + len > size) break;
     ix->frame.push_back(off);
     off += len;
   }
+  if (m) munmap(const_cast<uint8_t*>(m), (size_t)size);
   ix->end = off;
   if (ix->frame.empty()) {
     *err = std::string(path) + ": no XTC frame";
@@ -168,18 +178,30 @@ bool index_xtc(const char* path, XtcIndex* ix, std::string* err) {
 
 // ----------------------------------------------------------- device decode
 
-// Most-significant-first bit reader over one frame's compressed words.
+// Most-significant-first bit reader over one frame's compressed words. The
+// word after the one being consumed is already loaded, so its latency runs
+// under the decoding of the current word's bits.
 struct BitReader {
-  const uint32_t* w;
+  const uint32_t* w;  // next word to load
   const uint32_t* wend;
   uint64_t acc;  // unread bits, MSB-aligned
   int nacc;
-  uint32_t pos_words;  // words loaded
+  uint32_t next;       // the next word, loaded ahead (raw byte order)
+  uint32_t pos_words;  // words moved into acc
 
+  __device__ __forceinline__ void start(const uint32_t* first, const uint32_t* end) {
+    w = first;
+    wend = end;
+    acc = 0;
+    nacc = 0;
+    pos_words = 0;
+    next = w < wend ? __ldg(w) : 0u;
+    ++w;
+  }
   __device__ __forceinline__ uint32_t get(int n) {  // 1 <= n <= 32
     if (nacc < n) {
-      uint32_t v = 0;
-      if (w < wend) v = __byte_perm(__ldg(w), 0, 0x0123);
+      const uint32_t v = __byte_perm(next, 0, 0x0123);
+      next = w < wend ? __ldg(w) : 0u;
       ++w;
       ++pos_words;
       acc |= (uint64_t)v << (32 - nacc);
@@ -195,47 +217,80 @@ struct BitReader {
   }
 };
 
-// q = v / s, returns v % s; v = hi:mid:lo (s >= 1, s < 2^24).
-__device__ __forceinline__ uint32_t divmod96(uint32_t& hi, uint32_t& mid, uint32_t& lo,
-                                             uint32_t s) {
-  if ((hi | mid) == 0) {
-    const uint32_t q = lo / s;
-    const uint32_t r = lo - q * s;
-    lo = q;
-    return r;
+// Reciprocals m(s) = floor((2^64 - 1) / s) of the table's ranges, for
+// division by multiplication (Granlund and Montgomery, "Division by invariant
+// integers using multiplication", PLDI 1994).
+struct RangeInv {
+  uint64_t v[XTC_LAST];
+};
+constexpr RangeInv make_range_inv() {
+  RangeInv r{};
+  const int t[XTC_LAST] = XTC_RANGES;
+  for (int k = 0; k < XTC_LAST; ++k) r.v[k] = t[k] ? ~0ull / (uint64_t)t[k] : 0ull;
+  return r;
+}
+__constant__ RangeInv c_range_inv = make_range_inv();
+
+// q = t / s, returns t % s, for t < s 2^32 (so t < 2^56 and q < 2^32) and
+// m = floor((2^64 - 1) / s): the product estimate is q or q - 1.
+__device__ __forceinline__ uint32_t divrem_step(uint64_t t, uint32_t s, uint64_t m,
+                                                uint32_t* q) {
+  uint64_t qq = __umul64hi(t, m);
+  uint64_t r = t - qq * s;
+  if (r >= s) {
+    ++qq;
+    r -= s;
   }
-  const uint32_t qh = hi / s;
-  uint64_t r = hi - qh * s;
-  uint64_t t = (r << 32) | mid;
-  const uint32_t qm = (uint32_t)(t / s);
-  r = t - (uint64_t)qm * s;
-  t = (r << 32) | lo;
-  const uint32_t ql = (uint32_t)(t / s);
-  r = t - (uint64_t)ql * s;
-  hi = qh;
-  mid = qm;
-  lo = ql;
+  *q = (uint32_t)qq;
   return (uint32_t)r;
+}
+
+// v = hi:mid:lo becomes v / s; returns v % s (1 <= s < 2^24, m as above).
+__device__ __forceinline__ uint32_t divmod96(uint32_t& hi, uint32_t& mid, uint32_t& lo,
+                                             uint32_t s, uint64_t m) {
+  uint32_t r = 0;
+  if (hi) r = divrem_step(hi, s, m, &hi);
+  if (hi | mid) r = divrem_step(((uint64_t)r << 32) | mid, s, m, &mid);
+  return divrem_step(((uint64_t)r << 32) | lo, s, m, &lo);
 }
 
 // Three integers packed as N = (n0 s1 + n1) s2 + n2 in nbits bits, stored as
 // byte chunks least significant first, the last chunk holding what is left
 // of nbits (decodeints, xdrfile.c:708-741; n0 is the low 32 bits of the last
-// quotient). nbits <= 96.
-__device__ __forceinline__ void get_triple(BitReader& b, int nbits, uint32_t s0, uint32_t s1,
-                                           uint32_t s2, int32_t* n) {
+// quotient). Up to 64 bits the chunks are read with two reads and put in
+// order with a byte reversal; longer numbers chunk by chunk. nbits <= 96.
+__device__ __forceinline__ void get_triple(BitReader& b, int nbits, uint32_t s1, uint64_t m1,
+                                           uint32_t s2, uint64_t m2, int32_t* n) {
   uint32_t limb[3] = {0u, 0u, 0u};
-  int shift = 0;
-  while (nbits > 8) {
-    limb[shift >> 5] |= b.get(8) << (shift & 31);
-    shift += 8;
-    nbits -= 8;
+  if (nbits <= 64) {
+    const int k = (nbits - 1) >> 3;  // full byte chunks
+    const int r = nbits - 8 * k;     // bits of the last chunk, 1..8
+    uint64_t y = 0;                  // the k full chunks, first chunk most significant
+    if (k > 4) {
+      y = (uint64_t)b.get(32) << (8 * k - 32);
+      y |= b.get(8 * k - 32);
+    } else if (k > 0) {
+      y = b.get(8 * k);
+    }
+    const uint64_t last = b.get(r);
+    // reverse the chunk order: first chunk least significant
+    const uint64_t rev = ((uint64_t)__byte_perm((uint32_t)y, 0, 0x0123) << 32) |
+                         __byte_perm((uint32_t)(y >> 32), 0, 0x0123);
+    const uint64_t v = (k ? rev >> (64 - 8 * k) : 0ull) | (last << (8 * k));
+    limb[0] = (uint32_t)v;
+    limb[1] = (uint32_t)(v >> 32);
+  } else {
+    int shift = 0;
+    while (nbits > 8) {
+      limb[shift >> 5] |= b.get(8) << (shift & 31);
+      shift += 8;
+      nbits -= 8;
+    }
+    limb[shift >> 5] |= b.get(nbits) << (shift & 31);
   }
-  if (nbits > 0) limb[shift >> 5] |= b.get(nbits) << (shift & 31);
-  n[2] = (int32_t)divmod96(limb[2], limb[1], limb[0], s2);
-  n[1] = (int32_t)divmod96(limb[2], limb[1], limb[0], s1);
+  n[2] = (int32_t)divmod96(limb[2], limb[1], limb[0], s2, m2);
+  n[1] = (int32_t)divmod96(limb[2], limb[1], limb[0], s1, m1);
   n[0] = (int32_t)limb[0];
-  (void)s0;
 }
 
 __device__ __forceinline__ int32_t wadd(int32_t a, int32_t b) {
@@ -271,7 +326,7 @@ __device__ void xtc_fail(uint32_t* err, uint32_t code, uint32_t frame) {
 
 // One thread per frame; xdrfile_decompress_coord_float (xdrfile.c:761-961)
 // restated over a word-wise bit reader.
-__global__ void __launch_bounds__(XTC_DECODE_THREADS)
+__global__ void __launch_bounds__(XTC_DECODE_THREADS, 1)
     k_xtc_decode(const uint8_t* __restrict__ file, const uint64_t* __restrict__ frame_off,
                  uint32_t n_frames, uint32_t natoms, DecodeOut o, uint32_t* err) {
   const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
@@ -318,12 +373,10 @@ __global__ void __launch_bounds__(XTC_DECODE_THREADS)
     bitsize = hi ? 128 - __clzll(hi) : 64 - __clzll(lo);
   }
   const float inv = __double2float_rn(__ddiv_rn(1.0, (double)precision));
+  const uint64_t m1 = large ? 0ull : ~0ull / size[1];
+  const uint64_t m2 = large ? 0ull : ~0ull / size[2];
   BitReader b;
-  b.w = fw + 23;
-  b.wend = b.w + ((n_bytes + 3u) >> 2);
-  b.acc = 0;
-  b.nacc = 0;
-  b.pos_words = 0;
+  b.start(fw + 23, fw + 23 + ((n_bytes + 3u) >> 2));
   int smallnum = c_ranges[smallidx] / 2;
   int smaller = c_ranges[max(XTC_FIRST, smallidx - 1)] / 2;
   int run = 0;
@@ -334,7 +387,7 @@ __global__ void __launch_bounds__(XTC_DECODE_THREADS)
 #pragma unroll
       for (int d = 0; d < 3; ++d) big[d] = bits_d[d] ? (int32_t)b.get(bits_d[d]) : 0;
     } else {
-      get_triple(b, bitsize, size[0], size[1], size[2], big);
+      get_triple(b, bitsize, size[1], m1, size[2], m2, big);
     }
 #pragma unroll
     for (int d = 0; d < 3; ++d) big[d] = wadd(big[d], minint[d]);
@@ -351,10 +404,11 @@ __global__ void __launch_bounds__(XTC_DECODE_THREADS)
       ++i;
     } else {
       const uint32_t ss = (uint32_t)c_ranges[smallidx];
+      const uint64_t ms = c_range_inv.v[smallidx];
       int32_t prev[3] = {big[0], big[1], big[2]};
       for (uint32_t k = 0; k < n_small; ++k) {
         int32_t s[3];
-        get_triple(b, smallidx, ss, ss, ss, s);
+        get_triple(b, smallidx, ss, ms, ss, ms, s);
 #pragma unroll
         for (int d = 0; d < 3; ++d) s[d] = wadd(wadd(s[d], prev[d]), -smallnum);
         // the first small atom comes before the large one (the encoder
@@ -627,53 +681,45 @@ int column_map_xtc(uint32_t natoms, const size_t* usecols, size_t n_usecols,
   return ENT_OK;
 }
 
-// Copies [0, len) of the file to device memory d_file through two pinned
-// staging buffers; each buffer is filled by all host threads (pread) while
-// the other one's copy runs.
+// Copies [0, len) of the file to device memory d_file through the context's
+// two pinned staging buffers; each buffer is filled by all host threads
+// (pread) while the other one's copy runs.
 int upload_file(Ctx& c, const char* path, uint64_t len, uint8_t* d_file) {
   Fd f;
   f.fd = open(path, O_RDONLY);
   if (f.fd < 0) return c.fail(ENT_ERR_IO, std::string("cannot open ") + path);
-  const size_t CH = std::min<uint64_t>(len, 64ull << 20);
-  uint8_t* stage[2] = {nullptr, nullptr};
-  cudaEvent_t done[2] = {nullptr, nullptr};
-  int rc = ENT_OK;
-  for (int i = 0; i < 2 && rc == ENT_OK; ++i)
-    if (cudaHostAlloc(reinterpret_cast<void**>(&stage[i]), CH, cudaHostAllocDefault) !=
-            cudaSuccess ||
-        cudaEventCreateWithFlags(&done[i], cudaEventDisableTiming) != cudaSuccess)
-      rc = c.cuda_fail(cudaGetLastError(), "pinned staging");
+  const size_t CH = (size_t)std::min<uint64_t>(len, 32ull << 20);
+  int rc = c.ensure_staging(CH);
+  if (rc) return rc;
   const unsigned T = host_threads();
   uint64_t blk = 0;
   for (uint64_t off = 0; rc == ENT_OK && off < len; off += CH, ++blk) {
     const size_t n = (size_t)std::min<uint64_t>(CH, len - off);
     const int b = (int)(blk & 1);
-    if (blk >= 2 && cudaEventSynchronize(done[b]) != cudaSuccess) {
+    uint8_t* stage = c.h_stage[b];
+    if (blk >= 2 && cudaEventSynchronize(c.ev_stage[b]) != cudaSuccess) {
       rc = c.cuda_fail(cudaGetLastError(), "staging reuse");
       break;
     }
     const unsigned nt = (unsigned)std::min<size_t>(T, std::max<size_t>(1, n >> 20));
     std::vector<std::thread> th;
     std::vector<char> ok(nt, 1);
-    for (unsigned t = 0; t < nt; ++t) {
+    for (unsigned t = 1; t < nt; ++t) {
       const size_t a = n * t / nt, e = n * (t + 1) / nt;
-      th.emplace_back([&, a, e, t] { ok[t] = pread_all(f.fd, stage[b] + a, e - a, off + a); });
+      th.emplace_back([&, a, e, t] { ok[t] = pread_all(f.fd, stage + a, e - a, off + a); });
     }
+    ok[0] = pread_all(f.fd, stage, n / nt, off);
     for (auto& x : th) x.join();
     if (std::find(ok.begin(), ok.end(), 0) != ok.end()) {
       rc = c.fail(ENT_ERR_IO, "read failed");
       break;
     }
-    cudaError_t e = cudaMemcpyAsync(d_file + off, stage[b], n, cudaMemcpyHostToDevice, c.stream);
-    if (e == cudaSuccess) e = cudaEventRecord(done[b], c.stream);
+    cudaError_t e = cudaMemcpyAsync(d_file + off, stage, n, cudaMemcpyHostToDevice, c.stream);
+    if (e == cudaSuccess) e = cudaEventRecord(c.ev_stage[b], c.stream);
     if (e != cudaSuccess) rc = c.cuda_fail(e, "copy file block");
   }
   if (cudaStreamSynchronize(c.stream) != cudaSuccess && rc == ENT_OK)
     rc = c.cuda_fail(cudaGetLastError(), "copy file");
-  for (int i = 0; i < 2; ++i) {
-    if (stage[i]) cudaFreeHost(stage[i]);
-    if (done[i]) cudaEventDestroy(done[i]);
-  }
   return rc;
 }
 
