@@ -381,10 +381,14 @@ __global__ void k_m2_chunks(const Mom2D* __restrict__ ms, uint32_t n_inst,
   }
 }
 
-// P[k] = sum_{j<k} moments(pts[j]), k = 0..n
+// P[k] = sum_{j<k} moments(pts[j]), k = 0..n. Each thread sums M2_E
+// consecutive points; the rows of one e (point k0 + e of every lane) pass
+// through shared memory, so that every store instruction writes four whole
+// 128-byte rows instead of 16 bytes into each of 32 rows.
 __global__ void __launch_bounds__(M2_PT)
     k_m2_write(const Mom2D* __restrict__ ms, const u128* __restrict__ off) {
   __shared__ u128 sw[M2_PT / 32][NM];
+  __shared__ u128 stage[M2_PT / 32][32 * NM];  // one row per lane, chunks swizzled
   const Mom2D& M = ms[blockIdx.y];
   const uint64_t b0 = (uint64_t)blockIdx.x * M2_CHUNK;
   if (b0 >= M.n) return;  // block-uniform
@@ -407,16 +411,31 @@ __global__ void __launch_bounds__(M2_PT)
   if (b0 == 0 && threadIdx.x == 0)
 #pragma unroll
     for (int m = 0; m < NM; ++m) P[m] = 0;
-  for (uint32_t e = 0; e < M2_E; ++e)
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  u128* st = stage[warp];
+  // the warp's first point; lane r's rows are points wk0 + 8 r + e
+  const uint64_t wk0 = b0 + (uint64_t)(warp * 32) * M2_E;
+  for (uint32_t e = 0; e < M2_E; ++e) {
     if (k0 + e < M.n) {
       u128 q[NM];
       moments(M.pts[k0 + e], q);
 #pragma unroll
       for (int m = 0; m < NM; ++m) {
         run[m] += q[m];
-        P[NM * (k0 + e + 1) + m] = run[m];
+        st[lane * NM + (m ^ (lane & 7))] = run[m];
       }
     }
+    __syncwarp();
+    // 8 lanes per row: chunk c of row r = 4 i + lane / 8
+    const int c = lane & 7;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int r = 4 * i + (lane >> 3);
+      const uint64_t k = wk0 + (uint64_t)r * M2_E + e;
+      if (k < M.n) P[NM * (k + 1) + c] = st[r * NM + (c ^ (r & 7))];
+    }
+    __syncwarp();
+  }
 }
 
 __device__ __forceinline__ bool insup(float a, float b, float g2) {
