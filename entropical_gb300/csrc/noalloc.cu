@@ -18,8 +18,7 @@
 //
 // The device address of the array is looked up once per device, by the
 // first call made with that device current (cudaGetSymbolAddress), and
-// cached; that first call should come before any stream capture. With CUDA's
-// lazy module loading (the default) that first call also loads this
+// cached. With CUDA's lazy module loading (the default) that first call also loads this
 // library's device code and the array onto the device, so a service that
 // must not allocate after start-up should make one warm-up call then. Every
 // call is synchronous: it copies a few small tables from its own stack and

@@ -493,10 +493,9 @@ int ent_hestimate_batch(ent_ctx* ctx, const ent_instance* inst, size_t n_inst,
  * and d_out (n doubles) are device memory of the current device; stream may
  * be NULL. The call is synchronous (it waits for its work on the stream
  * before returning) and calls no allocator. The first call on a device looks
- * up the array's device address and should come before any stream capture;
- * with CUDA's lazy module loading it also loads this library's device code
- * and the array, so a caller that must not allocate after start-up makes one
- * warm-up call then. Calls share the array: calls that overlap on the GPU
+ * up the array's device address; with CUDA's lazy module loading it also
+ * loads this library's device code and the array, so a caller that must not
+ * allocate after start-up makes one warm-up call then. Calls share the array: calls that overlap on the GPU
  * race and must be serialised by the caller.
  */
 int ent_density_1d_noalloc(const float* d_x, size_t n, float h, double* d_out,
