@@ -704,7 +704,7 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
       launches += 1 + 3 * (strip_bits / 8);
     }
     // 5. strips, tiles, points, plan
-    if ((r = launch_strip_bounds(st, di, ni, max_n)) != cudaSuccess) return r;
+    if ((r = launch_strip_bounds(st, di, ni, max_strips)) != cudaSuccess) return r;
     if ((r = launch_tile_offsets(st, di, ni)) != cudaSuccess) return r;
     if ((r = launch_gather_pts(st, di, ni, max_n)) != cudaSuccess) return r;
     if ((r = cudaMemsetAsync(dnsrc, 0, sizeof(uint64_t) * 3, st)) != cudaSuccess) return r;

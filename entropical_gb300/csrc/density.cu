@@ -114,6 +114,10 @@ __device__ __forceinline__ uint32_t cell_of(float x, float lo, float inv_w, uint
   return a > 0.f ? (uint32_t)a : 0u;
 }
 
+// Four points per thread per step, their loads issued together (the
+// coordinate reads are gathers through the sorted order).
+constexpr uint32_t CL_ITEMS = 4;
+
 __global__ void k_strip_keys(const InstDev* __restrict__ insts,
                              const uint32_t* __restrict__ inst_ids,
                              const uint64_t* __restrict__ seg_off,
@@ -121,29 +125,54 @@ __global__ void k_strip_keys(const InstDev* __restrict__ insts,
                              uint32_t* __restrict__ vals) {
   const InstDev& I = insts[inst_ids[blockIdx.y]];
   const uint64_t base = seg_off[blockIdx.y];
-  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < I.n;
-       k += gridDim.x * blockDim.x) {
-    const uint32_t j = I.perm0[k];
-    uint32_t key = cell_of(I.x[1][j], I.lo1, I.inv_w1, I.ncell1);
-    if (I.d == 3) key = key * I.ncell2 + cell_of(I.x[2][j], I.lo2, I.inv_w2, I.ncell2);
-    keys[base + k] = key;
-    vals[base + k] = j;
+  const uint32_t n = I.n, stride = gridDim.x * blockDim.x;
+  const uint32_t* __restrict__ perm0 = I.perm0;
+  const float* __restrict__ x1 = I.x[1];
+  const float* __restrict__ x2 = I.x[2];
+  for (uint32_t k0 = blockIdx.x * blockDim.x + threadIdx.x; k0 < n; k0 += CL_ITEMS * stride) {
+    uint32_t j[CL_ITEMS];
+    float a[CL_ITEMS], b[CL_ITEMS];
+#pragma unroll
+    for (uint32_t u = 0; u < CL_ITEMS; ++u) {
+      const uint32_t k = k0 + u * stride;
+      j[u] = k < n ? perm0[k] : 0u;
+    }
+#pragma unroll
+    for (uint32_t u = 0; u < CL_ITEMS; ++u) {
+      const uint32_t k = k0 + u * stride;
+      a[u] = k < n ? x1[j[u]] : 0.f;
+      b[u] = (k < n && I.d == 3) ? x2[j[u]] : 0.f;
+    }
+#pragma unroll
+    for (uint32_t u = 0; u < CL_ITEMS; ++u) {
+      const uint32_t k = k0 + u * stride;
+      if (k >= n) break;
+      uint32_t key = cell_of(a[u], I.lo1, I.inv_w1, I.ncell1);
+      if (I.d == 3) key = key * I.ncell2 + cell_of(b[u], I.lo2, I.inv_w2, I.ncell2);
+      keys[base + k] = key;
+      vals[base + k] = j[u];
+    }
   }
 }
 
+// strip_start[s] = the first sorted position whose strip key is >= s, for
+// s = 0 .. n_strips: one lower-bound search per strip (a few hundred strips
+// per instance) instead of a pass over every point.
 __global__ void k_strip_bounds(const InstDev* __restrict__ insts) {
   const InstDev& I = insts[blockIdx.y];
-  const uint32_t n = I.n;
-  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k <= n;
-       k += gridDim.x * blockDim.x) {
-    if (I.d == 1) {
-      if (k == 0) I.strip_start[0] = 0;
-      if (k == n) I.strip_start[1] = n;
+  const uint32_t n = I.n, L = I.n_strips;
+  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s <= L;
+       s += gridDim.x * blockDim.x) {
+    if (I.d == 1) {  // one strip
+      I.strip_start[s] = s ? n : 0u;
       continue;
     }
-    const int64_t prev = (k == 0) ? -1 : (int64_t)I.skeys[k - 1];
-    const int64_t cur = (k == n) ? (int64_t)I.n_strips : (int64_t)I.skeys[k];
-    for (int64_t s = prev + 1; s <= cur; ++s) I.strip_start[s] = k;
+    uint32_t lo = 0, hi = n;
+    while (lo < hi) {
+      const uint32_t m = lo + ((hi - lo) >> 1);
+      if (I.skeys[m] < s) lo = m + 1; else hi = m;
+    }
+    I.strip_start[s] = lo;
   }
 }
 
@@ -190,18 +219,37 @@ __global__ void __launch_bounds__(1024) k_tile_offsets(const InstDev* __restrict
 
 __global__ void k_gather_pts(const InstDev* __restrict__ insts) {
   const InstDev& I = insts[blockIdx.y];
-  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < I.n;
-       k += gridDim.x * blockDim.x) {
-    const uint32_t j = I.perm[k];
-    // multiplication by a power of two is exact
-    const float y0 = I.x[0][j] * I.sc[0];
-    if (I.d == 1) {
-      reinterpret_cast<float*>(I.pts)[k] = y0;
-    } else if (I.d == 2) {
-      reinterpret_cast<float2*>(I.pts)[k] = make_float2(y0, I.x[1][j] * I.sc[1]);
-    } else {
-      reinterpret_cast<float4*>(I.pts)[k] =
-          make_float4(y0, I.x[1][j] * I.sc[1], I.x[2][j] * I.sc[2], 0.f);
+  const uint32_t n = I.n, stride = gridDim.x * blockDim.x;
+  const int d = (int)I.d;
+  const uint32_t* __restrict__ perm = I.perm;
+  for (uint32_t k0 = blockIdx.x * blockDim.x + threadIdx.x; k0 < n; k0 += CL_ITEMS * stride) {
+    uint32_t j[CL_ITEMS];
+    float v[CL_ITEMS][3];
+#pragma unroll
+    for (uint32_t u = 0; u < CL_ITEMS; ++u) {
+      const uint32_t k = k0 + u * stride;
+      j[u] = k < n ? perm[k] : 0u;
+    }
+#pragma unroll
+    for (uint32_t u = 0; u < CL_ITEMS; ++u) {
+      const bool in = k0 + u * stride < n;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) v[u][c] = (in && c < d) ? I.x[c][j[u]] : 0.f;
+    }
+#pragma unroll
+    for (uint32_t u = 0; u < CL_ITEMS; ++u) {
+      const uint32_t k = k0 + u * stride;
+      if (k >= n) break;
+      // multiplication by a power of two is exact
+      const float y0 = v[u][0] * I.sc[0];
+      if (d == 1) {
+        reinterpret_cast<float*>(I.pts)[k] = y0;
+      } else if (d == 2) {
+        reinterpret_cast<float2*>(I.pts)[k] = make_float2(y0, v[u][1] * I.sc[1]);
+      } else {
+        reinterpret_cast<float4*>(I.pts)[k] =
+            make_float4(y0, v[u][1] * I.sc[1], v[u][2] * I.sc[2], 0.f);
+      }
     }
   }
 }
@@ -774,15 +822,15 @@ cudaError_t launch_strip_keys(cudaStream_t st, const InstDev* insts,
                               uint32_t n_seg, uint32_t max_n, uint32_t* keys,
                               uint32_t* vals) {
   if (n_seg == 0) return cudaSuccess;
-  k_strip_keys<<<dim3(grid_x_for(max_n), n_seg), 256, 0, st>>>(
+  k_strip_keys<<<dim3(grid_x_for((max_n + CL_ITEMS - 1) / CL_ITEMS), n_seg), 256, 0, st>>>(
       insts, inst_ids, seg_off, keys, vals);
   return cudaGetLastError();
 }
 
 cudaError_t launch_strip_bounds(cudaStream_t st, const InstDev* insts,
-                                uint32_t n_inst, uint32_t max_n) {
+                                uint32_t n_inst, uint32_t max_strips) {
   if (n_inst == 0) return cudaSuccess;
-  k_strip_bounds<<<dim3(grid_x_for(max_n + 1), n_inst), 256, 0, st>>>(insts);
+  k_strip_bounds<<<dim3(grid_x_for(max_strips + 1), n_inst), 256, 0, st>>>(insts);
   return cudaGetLastError();
 }
 
@@ -796,7 +844,8 @@ cudaError_t launch_tile_offsets(cudaStream_t st, const InstDev* insts,
 cudaError_t launch_gather_pts(cudaStream_t st, const InstDev* insts,
                               uint32_t n_inst, uint32_t max_n) {
   if (n_inst == 0) return cudaSuccess;
-  k_gather_pts<<<dim3(grid_x_for(max_n), n_inst), 256, 0, st>>>(insts);
+  k_gather_pts<<<dim3(grid_x_for((max_n + CL_ITEMS - 1) / CL_ITEMS), n_inst), 256, 0, st>>>(
+      insts);
   return cudaGetLastError();
 }
 

@@ -108,8 +108,9 @@ cudaError_t launch_strip_keys(cudaStream_t st, const InstDev* insts,
                               const uint32_t* inst_ids, const uint64_t* seg_off,
                               uint32_t n_seg, uint32_t max_n, uint32_t* keys,
                               uint32_t* vals);
+// strip_start of every instance (max_strips: the largest n_strips)
 cudaError_t launch_strip_bounds(cudaStream_t st, const InstDev* insts,
-                                uint32_t n_inst, uint32_t max_n);
+                                uint32_t n_inst, uint32_t max_strips);
 cudaError_t launch_tile_offsets(cudaStream_t st, const InstDev* insts,
                                 uint32_t n_inst);
 cudaError_t launch_gather_pts(cudaStream_t st, const InstDev* insts,

@@ -206,7 +206,7 @@ extern "C" int ent_density_1d_noalloc(const float* d_x, size_t n, float h, doubl
       cudaMemcpyAsync(S + O_BASE, &base0, 4, cudaMemcpyHostToDevice, st) != cudaSuccess)
     return cuda_error();
   TileDesc* tiles = reinterpret_cast<TileDesc*>(S + O_TILES);
-  if (launch_strip_bounds(st, dinst, 1, nn) != cudaSuccess ||
+  if (launch_strip_bounds(st, dinst, 1, I.n_strips) != cudaSuccess ||
       launch_tile_offsets(st, dinst, 1) != cudaSuccess ||
       launch_gather_pts(st, dinst, 1, nn) != cudaSuccess ||
       launch_plan(st, dinst, 1, reinterpret_cast<const uint32_t*>(S + O_BASE), tiles, I.tile_cap,
