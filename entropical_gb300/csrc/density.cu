@@ -278,12 +278,14 @@ __device__ uint32_t upper_y(const void* pts, int d, uint32_t a, uint32_t b, floa
   return a;
 }
 
-__global__ void k_plan(const InstDev* __restrict__ insts, uint32_t n_inst,
-                       const uint32_t* __restrict__ inst_tile_base,
-                       TileDesc* __restrict__ tiles, uint32_t n_slots,
-                       unsigned long long* __restrict__ n_src_total) {
-  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= n_slots) return;
+// The plan of slot g: its tile descriptor; returns the slot's candidate
+// pairs (sources x targets) and its dimension in *d_out (left 0 for an empty
+// slot).
+__device__ __forceinline__ unsigned long long plan_slot(const InstDev* __restrict__ insts,
+                                                        uint32_t n_inst,
+                                                        const uint32_t* __restrict__ inst_tile_base,
+                                                        TileDesc* __restrict__ tiles, uint32_t g,
+                                                        int* d_out) {
   uint32_t lo = 0, hi = n_inst;
   while (hi - lo > 1) {
     const uint32_t m = (lo + hi) / 2;
@@ -303,7 +305,7 @@ __global__ void k_plan(const InstDev* __restrict__ insts, uint32_t n_inst,
   const uint32_t total = I.tile_off[I.n_strips];
   if (t >= total) {
     tiles[g] = td;
-    return;
+    return 0ull;
   }
   uint32_t a = 0, b = I.n_strips;
   while (b - a > 1) {
@@ -318,7 +320,7 @@ __global__ void k_plan(const InstDev* __restrict__ insts, uint32_t n_inst,
   const uint32_t tb = max(tb0, I.t_lo), te = min(te0, I.t_hi);
   if (te <= tb) {  // outside the share
     tiles[g] = td;
-    return;
+    return 0ull;
   }
   const uint32_t tc = te - tb;
   const float yf = y0_at(I.pts, d, tb);
@@ -393,7 +395,26 @@ __global__ void k_plan(const InstDev* __restrict__ insts, uint32_t n_inst,
     nsrc = b - a;
   }
   tiles[g] = td;
-  if (n_src_total) atomicAdd(n_src_total + (d - 1), nsrc * (unsigned long long)tc);
+  *d_out = d;
+  return nsrc * (unsigned long long)tc;
+}
+
+// One thread per slot. The candidate-pair totals are summed per warp and
+// dimension first: one atomic per warp, not one per slot on one address.
+__global__ void k_plan(const InstDev* __restrict__ insts, uint32_t n_inst,
+                       const uint32_t* __restrict__ inst_tile_base,
+                       TileDesc* __restrict__ tiles, uint32_t n_slots,
+                       unsigned long long* __restrict__ n_src_total) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  int d = 0;
+  const unsigned long long c =
+      g < n_slots ? plan_slot(insts, n_inst, inst_tile_base, tiles, g, &d) : 0ull;
+  if (!n_src_total) return;  // grid-uniform
+  for (int dd = 1; dd <= 3; ++dd) {
+    unsigned long long v = d == dd ? c : 0ull;
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(n_src_total + (dd - 1), v);
+  }
 }
 
 // ------------------------------------------------------- pair kernel
