@@ -122,11 +122,12 @@ void te_build(const Ctx& c, const float* dc, size_t n_rows, size_t M, const floa
     for (size_t i = 0; i < M; ++i)
       for (size_t j = 0; j < M; ++j)
         if (i != j) {
-          mk(3, v0 + M + i, v0 + i, v0 + j, h[i], h[i], h[j]);
-          // (y+, y, x): y follows the sorted y+ closely, so cells of h
-          // suffice there; x is independent and gets cells of h/2
-          // (3 x 5 strips; 3-D kernel on the 32 x 200k, 3-lag batch
-          // 815 -> 776 ms against 3 x 3)
+          // (x, y+, y): x sorted, cells of h in y+ and h/2 in y (3 x 5
+          // strips). The same density as (y+, y, x), with y+ sorted and
+          // cells in y and x, and the same candidates, but the 3-D kernel
+          // on the 32 x 200k, 3-lag batch takes 740 ms against 770 ms (and
+          // 751 ms with cells of h in both, 780 ms with h/2 in both).
+          mk(3, v0 + j, v0 + M + i, v0 + i, h[j], h[i], h[i]);
           insts->back().S3[0] = 1;
           insts->back().S3[1] = 2;
         }

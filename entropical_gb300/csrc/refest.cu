@@ -353,10 +353,12 @@ int ent_reference_estimator(ent_ctx* ctx, const float* coords, size_t n_rows, si
         const float hh[2] = {h[i], h[j]};
         pij[i * M + j] = B.add(2, cc, z, hh);
         if (estimator == ENT_REF_TRANSS) {
-          const size_t ca[3] = {i, i, j};
-          const uint32_t la[3] = {0, tau, 0};
-          const float ha[3] = {h[i], h[i], h[j]};
-          // (x_i, x_i+tau, x_j): dimension 1 follows the sorted dimension 0
+          // the density of (x_i, x_i+tau, x_j) as (x_j, x_i, x_i+tau): the
+          // independent coordinate sorted, cells of h and h/2 in the two
+          // that follow each other (the order the TE batch measured fastest)
+          const size_t ca[3] = {j, i, i};
+          const uint32_t la[3] = {0, 0, tau};
+          const float ha[3] = {h[j], h[i], h[i]};
           p3a[i * M + j] = B.add(3, ca, la, ha, 1, 2);  // p_ij_itau
           const size_t cb[3] = {i, j, j};
           const uint32_t lb[3] = {0, 0, tau};
