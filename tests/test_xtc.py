@@ -130,3 +130,15 @@ def test_against_reference_codec(tmp_path, seed):
         write_xtc(pm, rows.T.copy())
         assert Path(pm).read_bytes() == Path(pr).read_bytes(), (kind, n_atoms)
         assert np.array_equal(_bits(O.read_xtc(pm)), _bits(O.ref_read_xtc(pr, n_atoms)))
+
+
+def test_writer_row_major_input(xg, tmp_path):
+    """primary 'R' (one row per frame) writes the same bytes as the
+    column-major input."""
+    rows = xg["water_in"]
+    pc, pr = str(tmp_path / "c.xtc"), str(tmp_path / "r.xtc")
+    write_xtc(pc, rows.T.copy())
+    write_xtc(pr, rows, primary="R")
+    assert Path(pr).read_bytes() == Path(pc).read_bytes() == xg["water_bytes"].tobytes()
+    with pytest.raises(ValueError):
+        write_xtc(pr, rows, primary="X")
