@@ -2,7 +2,7 @@
 
 Compiles every ``csrc/*.cu`` translation unit with nvcc in parallel and links
 ``lib/libentropical_gb300.so``; compiles the C++ drop-in shim
-(``shim/densities_gb300.cpp``) into ``lib/libentropical_shim.so``. No cmake,
+(``shim/densities_gb300.cpp``, ``shim/coords_file_gb300.cpp``) into ``lib/libentropical_shim.so``. No cmake,
 no torch extension machinery: plain nvcc/g++ invocations, so the same recipe
 runs on the x86_64 build host and on the aarch64 GPU hosts.
 """
@@ -76,13 +76,14 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     out = lib_path()
     if force or _stale(out, objs):
         _run([nvcc, *ARCH, "-shared", "-o", str(out), *map(str, objs), "-lcudart"])
-    shim_src = SHIM / "densities_gb300.cpp"
-    if shim_src.exists():
+    shim_srcs = [SHIM / "densities_gb300.cpp", SHIM / "coords_file_gb300.cpp"]
+    if all(p.exists() for p in shim_srcs):
         sout = shim_path()
-        deps = [shim_src, SHIM / "densities_gb300.hpp", INCLUDE / "entropical_gb300.h", out]
+        deps = [*shim_srcs, SHIM / "densities_gb300.hpp", SHIM / "coords_file_gb300.hpp",
+                INCLUDE / "entropical_gb300.h", out]
         if force or _stale(sout, deps):
             _run(["g++", "-std=c++14", "-O2", "-fPIC", "-shared", "-I", str(INCLUDE), "-I", str(SHIM),
-                  str(shim_src), "-o", str(sout), "-L", str(LIB), "-lentropical_gb300",
+                  *map(str, shim_srcs), "-o", str(sout), "-L", str(LIB), "-lentropical_gb300",
                   "-Wl,-rpath,$ORIGIN"])
     if verbose:
         print("built", out)
