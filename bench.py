@@ -72,6 +72,8 @@ def parse():
                     help="time only the XTC trajectory load (1000 atoms x N frames): the small "
                          "case for ncu captures of the decode kernel; prints a JSON line of its "
                          "own")
+    ap.add_argument("--xtc-atoms", type=int, default=1000,
+                    help="atoms of the --xtc-frames trajectory (default 1000)")
     ap.add_argument("--coords", type=int, default=N_COORDS,
                     help="coordinates of the MI batch (64 = the benchmark workload; "
                          "smaller values give the small case used for ncu captures)")
@@ -643,9 +645,10 @@ def other_configs(ctx):
 
 
 def xtc_trajectory(n_atoms: int, n_frames: int, seed: int = 21) -> np.ndarray:
-    """Synthetic MD-like frames (n_frames, 3 n_atoms): a 250-atom chain with
-    0.15 nm steps drifting as a whole, and 250 three-atom water molecules in
-    a 5 nm box, every atom jittered by 0.03 nm per frame."""
+    """Synthetic MD-like frames (n_frames, 3 n_atoms): a chain of a quarter of
+    the atoms with 0.15 nm steps drifting as a whole, and three-atom water
+    molecules for the rest in a 5 nm box, every atom jittered by 0.03 nm per
+    frame."""
     rng = np.random.default_rng(seed)
     n_chain = n_atoms // 4
     n_mol = (n_atoms - n_chain) // 3
@@ -668,7 +671,8 @@ def xtc_config(ctx, n_atoms: int = 1000, n_frames: int = 50_000):
     """XTC trajectory input (CoordsFile::XtcHandler, coords_file.cpp:70-126):
     write a synthetic trajectory with the library's writer, then load it into
     a column-major device matrix (ent_load_xtc_device: host index, pinned
-    copies of the compressed file, one decoding thread per frame). Times the
+    copies of the compressed file, a walk per frame, one decoding thread per
+    64-atom segment). Times the
     load (best of 3, wall, from the page cache) and the decode kernel, checks
     sampled frames against the oracle's reader bit for bit, and times the
     oracle's serial reader (the reference reads frame by frame with read_xtc)
@@ -700,7 +704,7 @@ def xtc_config(ctx, n_atoms: int = 1000, n_frames: int = 50_000):
         t0 = time.perf_counter()
         xtc_file_shape(path)
         t_index = time.perf_counter() - t0
-        sample = 2000
+        sample = min(2000, n_frames)
         got = dev[:, :sample].cpu().numpy()
         t0 = time.perf_counter()
         want = O.read_xtc(path, 0, sample)
@@ -817,7 +821,7 @@ def main():
         return te_only(args)
     if args.xtc_frames:
         from entropical_gb300 import Context
-        print(json.dumps(xtc_config(Context(), n_frames=args.xtc_frames)))
+        print(json.dumps(xtc_config(Context(), n_atoms=args.xtc_atoms, n_frames=args.xtc_frames)))
         return None
     ws, rank, local = dist_env()
     from entropical_gb300 import workloads

@@ -7,13 +7,17 @@
 // XTC, vendored by the reference as xdrfile (Frans van Hoesel's coordinate
 // compression: xdrfile.c:761-961 decodes, :963-1255 encodes).
 //
-// Reading, GB300-first: frames are independent, so the file is indexed on
-// the host (one pass over the frame headers), copied whole to device memory
-// through pinned staging buffers filled by all host threads, and decoded by
-// one thread per frame straight into the column-major coordinate matrix the
-// density calls take (column 3a + c holds coordinate c of atom a over all
-// frames, so the 32 frames of a warp write consecutive addresses). The
-// compressed file is what crosses the host link, not the floats.
+// Reading, GB300-first: the file is indexed on the host (one pass over the
+// frame headers) and copied whole to device memory through pinned staging
+// buffers filled by all host threads; what crosses the host link is the
+// compressed file, not the floats. Each frame is one serial bit stream (the
+// position of every atom group follows from the groups before it), so the
+// device decodes in two passes: a walk per frame reads only the flag and run
+// bits, validates the frame and records the decoder's state at every 64th
+// atom; then one thread per 64-atom segment decodes the packed values
+// straight into the column-major coordinate matrix the density calls take
+// (column 3a + c holds coordinate c of atom a over all frames; threads of
+// consecutive frames write neighbouring addresses).
 //
 // Frame layout (XDR: big-endian 4-byte units): magic 1995, natoms, step,
 // time, box[9], natoms again; natoms <= 9: 3 * natoms raw floats; else
@@ -178,23 +182,28 @@ bool index_xtc(const char* path, XtcIndex* ix, std::string* err) {
 
 // ----------------------------------------------------------- device decode
 
-// Most-significant-first bit reader over one frame's compressed words. The
-// word after the one being consumed is already loaded, so its latency runs
-// under the decoding of the current word's bits.
+// Most-significant-first bit reader over one frame's compressed words,
+// started at any bit position. The word after the one being consumed is
+// already loaded, so its latency runs under the decoding of the current
+// word's bits. Words past the frame's data read as zero.
 struct BitReader {
   const uint32_t* w;  // next word to load
   const uint32_t* wend;
   uint64_t acc;  // unread bits, MSB-aligned
   int nacc;
-  uint32_t next;       // the next word, loaded ahead (raw byte order)
-  uint32_t pos_words;  // words moved into acc
+  uint32_t next;  // the next word, loaded ahead (raw byte order)
+  uint64_t pos;   // bits consumed from the start of the data
 
-  __device__ __forceinline__ void start(const uint32_t* first, const uint32_t* end) {
-    w = first;
+  __device__ __forceinline__ void start(const uint32_t* data, const uint32_t* end,
+                                        uint64_t bitpos) {
+    w = data + (bitpos >> 5);
     wend = end;
-    acc = 0;
-    nacc = 0;
-    pos_words = 0;
+    pos = bitpos;
+    const uint32_t first = w < wend ? __byte_perm(__ldg(w), 0, 0x0123) : 0u;
+    ++w;
+    const int skip = (int)(bitpos & 31u);
+    acc = ((uint64_t)first << 32) << skip;
+    nacc = 32 - skip;
     next = w < wend ? __ldg(w) : 0u;
     ++w;
   }
@@ -203,17 +212,14 @@ struct BitReader {
       const uint32_t v = __byte_perm(next, 0, 0x0123);
       next = w < wend ? __ldg(w) : 0u;
       ++w;
-      ++pos_words;
       acc |= (uint64_t)v << (32 - nacc);
       nacc += 32;
     }
     const uint32_t v = (uint32_t)(acc >> (64 - n));
     acc <<= n;
     nacc -= n;
+    pos += (uint64_t)n;
     return v;
-  }
-  __device__ __forceinline__ uint64_t consumed_bits() const {
-    return 32ull * pos_words - (uint64_t)nacc;
   }
 };
 
@@ -318,79 +324,215 @@ enum : uint32_t {
   XERR_RANGE = 2,    // empty or 32-bit coordinate range
   XERR_ATOMS = 3,    // a run past the frame's atom count
   XERR_OVERRUN = 4,  // decoded past the byte count
+  XERR_BIG = 5,      // a compressed frame of 256 MB or more
 };
 
 __device__ void xtc_fail(uint32_t* err, uint32_t code, uint32_t frame) {
   if (atomicCAS(err, 0u, code) == 0u) err[1] = frame;
 }
 
-// One thread per frame; xdrfile_decompress_coord_float (xdrfile.c:761-961)
-// restated over a word-wise bit reader.
-__global__ void __launch_bounds__(XTC_DECODE_THREADS, 1)
-    k_xtc_decode(const uint8_t* __restrict__ file, const uint64_t* __restrict__ frame_off,
-                 uint32_t n_frames, uint32_t natoms, DecodeOut o, uint32_t* err) {
-  const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
-  if (f >= n_frames) return;
+// Atoms per decoding segment: the walk records the decoder's state at the
+// first atom group that starts at or after every multiple of XTC_SEG_ATOMS.
+constexpr uint32_t XTC_SEG_ATOMS = 64;
+
+// Decoder state at the start of an atom group: the bit position, the atom
+// index, the small-integer table index and the run length (which carries
+// over groups whose flag bit is 0). Nothing else crosses groups: the group's
+// large atom resets the previous coordinates.
+struct XtcCheckpoint {
+  uint64_t pos;
+  uint32_t atom;
+  uint16_t smallidx;
+  uint16_t run;
+};
+
+// The constants of one compressed frame (xdrfile.c:761-840).
+struct FrameHead {
+  const uint32_t* data;
+  const uint32_t* dend;
+  uint32_t n_bytes;
+  int32_t minint[3];
+  uint32_t size[3];
+  uint64_t m1, m2;  // reciprocals of size[1], size[2]
+  int bits_d[3];    // large ranges: bits per coordinate
+  int bitsize;      // else: bits of the packed triple
+  bool large;
+  float inv;
+  int smallidx;
+};
+
+__device__ __forceinline__ uint32_t be_word(const uint32_t* p) {
+  return __byte_perm(__ldg(p), 0, 0x0123);
+}
+
+// Header of frame f (natoms > 9); false (and err set) for a malformed one.
+__device__ bool parse_head(const uint32_t* fw, uint32_t f, FrameHead& h, uint32_t* err) {
+  const float precision = __uint_as_float(be_word(fw + 14));
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    h.minint[d] = (int32_t)be_word(fw + 15 + d);
+    h.size[d] = be_word(fw + 18 + d) - (uint32_t)h.minint[d] + 1u;
+  }
+  h.smallidx = (int32_t)be_word(fw + 21);
+  h.n_bytes = be_word(fw + 22);
+  h.data = fw + 23;
+  h.dend = h.data + ((h.n_bytes + 3u) >> 2);
+  if (h.smallidx < XTC_FIRST || h.smallidx >= XTC_LAST) {
+    xtc_fail(err, XERR_INDEX, f);
+    return false;
+  }
+  h.large = (h.size[0] | h.size[1] | h.size[2]) > 0xffffffu;
+  h.bitsize = 0;
+  h.m1 = h.m2 = 0;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) h.bits_d[d] = 0;
+  if (h.large) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      h.bits_d[d] = 32 - __clz(h.size[d]);  // smallest b with size < 2^b
+      if (h.bits_d[d] >= 32) {
+        xtc_fail(err, XERR_RANGE, f);
+        return false;
+      }
+    }
+  } else {
+    if (h.size[0] == 0u || h.size[1] == 0u || h.size[2] == 0u) {
+      xtc_fail(err, XERR_RANGE, f);
+      return false;
+    }
+    // bit length of size0 size1 size2 (< 2^72)
+    const uint64_t p01 = (uint64_t)h.size[0] * h.size[1];
+    const uint64_t lo = p01 * h.size[2];
+    const uint64_t hi = __umul64hi(p01, h.size[2]);
+    h.bitsize = hi ? 128 - __clzll(hi) : 64 - __clzll(lo);
+    h.m1 = ~0ull / h.size[1];
+    h.m2 = ~0ull / h.size[2];
+  }
+  h.inv = __double2float_rn(__ddiv_rn(1.0, (double)precision));
+  return true;
+}
+
+// Pass 1, one walk per frame: goes over the atom groups reading only what
+// decides the next group's position (the flag and run bits; the packed
+// values are passed over by their bit lengths), validates the frame and
+// records a checkpoint at the first group starting at or after every
+// multiple of XTC_SEG_ATOMS atoms. xdrfile_decompress_coord_float
+// (xdrfile.c:761-961) restated, without the arithmetic.
+// stride: threads per frame, 1 or 32. A warp's lanes wait for each other at
+// every step, and every step of a walk waits on its own load, so with few
+// frames each walk gets a warp of its own (stride 32: lane 0 walks) and waits
+// only for its own cache misses; with many frames the warps of 32 walks
+// hide each other's waits.
+__global__ void __launch_bounds__(XTC_DECODE_THREADS)
+    k_xtc_walk(const uint8_t* __restrict__ file, const uint64_t* __restrict__ frame_off,
+               uint32_t n_frames, uint32_t natoms, uint32_t max_seg, uint32_t stride,
+               XtcCheckpoint* __restrict__ cps, uint32_t* __restrict__ n_seg, uint32_t* err) {
+  const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid % stride) return;
+  const uint64_t fl = tid / stride;
+  if (fl >= n_frames) return;
+  const uint32_t f = (uint32_t)fl;
+  n_seg[f] = 0;
+  XtcCheckpoint* cp = cps + (size_t)f * max_seg;
+  if (natoms <= 9) {  // raw floats: one segment
+    cp[0] = XtcCheckpoint{0, 0, 0, 0};
+    n_seg[f] = 1;
+    return;
+  }
   const uint32_t* fw = reinterpret_cast<const uint32_t*>(file + frame_off[f]);
-  auto word = [&](int k) { return __byte_perm(__ldg(fw + k), 0, 0x0123); };
+  FrameHead h;
+  if (!parse_head(fw, f, h, err)) return;
+  const uint32_t big_bits =
+      h.large ? (uint32_t)(h.bits_d[0] + h.bits_d[1] + h.bits_d[2]) : (uint32_t)h.bitsize;
+  const uint32_t n_words = (uint32_t)(h.dend - h.data);
+  if (n_words >= (1u << 26)) return xtc_fail(err, XERR_BIG, f);  // bit positions < 2^31
+  // A serial chain per frame: every instruction waits for the one before,
+  // so the loop keeps to 32-bit positions, one funnel shift for the flag and
+  // run bits, and v / 3 as (11 v) >> 5 (exact for v < 32).
+  uint32_t pos = 0;
+  int smallidx = h.smallidx;
+  uint32_t n_small = 0;     // atoms of the current run (carried while the flag is 0)
+  uint32_t small_bits = 0;  // their bits: n_small * smallidx
+  uint32_t i = 0, seg = 0, next_cp = 0;
+  while (i < natoms) {
+    if (i >= next_cp) {
+      if (seg >= max_seg) return xtc_fail(err, XERR_ATOMS, f);  // cannot happen
+      cp[seg++] = XtcCheckpoint{pos, i, (uint16_t)smallidx, (uint16_t)(3u * n_small)};
+      next_cp = (i / XTC_SEG_ATOMS + 1) * XTC_SEG_ATOMS;
+    }
+    pos += big_bits;  // the group's large atom
+    const uint32_t wi = pos >> 5;
+    const uint32_t a = wi < n_words ? be_word(h.data + wi) : 0u;
+    const uint32_t b = wi + 1u < n_words ? be_word(h.data + wi + 1u) : 0u;
+    const uint32_t top = __funnelshift_l(b, a, pos & 31u);  // bits from pos on
+    int is_smaller = 0;
+    if (top >> 31) {  // flag: a new run length follows in 5 bits
+      const uint32_t v = (top >> 26) & 31u;
+      const uint32_t q = (v * 11u) >> 5;  // v / 3
+      is_smaller = (int)(v - 3u * q) - 1;
+      n_small = q;
+      small_bits = q * (uint32_t)smallidx;
+      pos += 6;
+    } else {
+      pos += 1;
+    }
+    if (i + 1u + n_small > natoms) return xtc_fail(err, XERR_ATOMS, f);
+    pos += small_bits;  // the group's small atoms
+    i += 1u + n_small;
+    if (is_smaller != 0) {
+      smallidx += is_smaller;
+      if (smallidx < XTC_FIRST || smallidx >= XTC_LAST) return xtc_fail(err, XERR_INDEX, f);
+      small_bits = n_small * (uint32_t)smallidx;
+    }
+  }
+  if ((uint64_t)pos > 8ull * h.n_bytes) return xtc_fail(err, XERR_OVERRUN, f);
+  n_seg[f] = seg;
+}
+
+// Pass 2, one thread per (segment, frame), frames fastest: decodes the atom
+// groups from its checkpoint to the next one and writes their atoms.
+__global__ void __launch_bounds__(XTC_DECODE_THREADS)
+    k_xtc_decode(const uint8_t* __restrict__ file, const uint64_t* __restrict__ frame_off,
+                 uint32_t n_frames, uint32_t natoms, uint32_t max_seg,
+                 const XtcCheckpoint* __restrict__ cps, const uint32_t* __restrict__ n_seg,
+                 DecodeOut o, uint32_t* err) {
+  const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (uint64_t)n_frames * max_seg) return;
+  const uint32_t f = (uint32_t)(t % n_frames), seg = (uint32_t)(t / n_frames);
+  const uint32_t ns = n_seg[f];
+  if (seg >= ns) return;
+  const uint32_t* fw = reinterpret_cast<const uint32_t*>(file + frame_off[f]);
   if (natoms <= 9) {
     for (uint32_t a = 0; a < natoms; ++a) {
       for (int c = 0; c < 3; ++c) {
         const int32_t col = o.col_map ? __ldg(o.col_map + 3 * a + c) : (int32_t)(3 * a + c);
         if (col >= 0)
           o.out[(size_t)col * o.col_stride + (size_t)f * o.row_stride] =
-              __uint_as_float(word(14 + 3 * a + c));
+              __uint_as_float(be_word(fw + 14 + 3 * a + c));
       }
     }
     return;
   }
-  const float precision = __uint_as_float(word(14));
-  int32_t minint[3];
-  uint32_t size[3];
-#pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    minint[d] = (int32_t)word(15 + d);
-    size[d] = word(18 + d) - (uint32_t)minint[d] + 1u;
-  }
-  int smallidx = (int32_t)word(21);
-  const uint32_t n_bytes = word(22);
-  if (smallidx < XTC_FIRST || smallidx >= XTC_LAST) return xtc_fail(err, XERR_INDEX, f);
-  const bool large = (size[0] | size[1] | size[2]) > 0xffffffu;
-  int bits_d[3] = {0, 0, 0};
-  int bitsize = 0;
-  if (large) {
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      bits_d[d] = 32 - __clz(size[d]);  // smallest b with size < 2^b
-      if (bits_d[d] >= 32) return xtc_fail(err, XERR_RANGE, f);
-    }
-  } else {
-    if (size[0] == 0u || size[1] == 0u || size[2] == 0u) return xtc_fail(err, XERR_RANGE, f);
-    // bit length of size0 size1 size2 (< 2^72)
-    const uint64_t p01 = (uint64_t)size[0] * size[1];
-    const uint64_t lo = p01 * size[2];
-    const uint64_t hi = __umul64hi(p01, size[2]);
-    bitsize = hi ? 128 - __clzll(hi) : 64 - __clzll(lo);
-  }
-  const float inv = __double2float_rn(__ddiv_rn(1.0, (double)precision));
-  const uint64_t m1 = large ? 0ull : ~0ull / size[1];
-  const uint64_t m2 = large ? 0ull : ~0ull / size[2];
+  FrameHead h;
+  if (!parse_head(fw, f, h, err)) return;
+  const XtcCheckpoint cp = cps[(size_t)f * max_seg + seg];
+  const uint32_t end = seg + 1 < ns ? cps[(size_t)f * max_seg + seg + 1].atom : natoms;
   BitReader b;
-  b.start(fw + 23, fw + 23 + ((n_bytes + 3u) >> 2));
+  b.start(h.data, h.dend, cp.pos);
+  int smallidx = cp.smallidx;
   int smallnum = c_ranges[smallidx] / 2;
-  int smaller = c_ranges[max(XTC_FIRST, smallidx - 1)] / 2;
-  int run = 0;
-  uint32_t i = 0;
-  while (i < natoms) {
+  int run = cp.run;
+  uint32_t i = cp.atom;
+  while (i < end) {
     int32_t big[3];
-    if (large) {
+    if (h.large) {
 #pragma unroll
-      for (int d = 0; d < 3; ++d) big[d] = bits_d[d] ? (int32_t)b.get(bits_d[d]) : 0;
+      for (int d = 0; d < 3; ++d) big[d] = h.bits_d[d] ? (int32_t)b.get(h.bits_d[d]) : 0;
     } else {
-      get_triple(b, bitsize, size[1], m1, size[2], m2, big);
+      get_triple(b, h.bitsize, h.size[1], h.m1, h.size[2], h.m2, big);
     }
 #pragma unroll
-    for (int d = 0; d < 3; ++d) big[d] = wadd(big[d], minint[d]);
+    for (int d = 0; d < 3; ++d) big[d] = wadd(big[d], h.minint[d]);
     int is_smaller = 0;
     if (b.get(1)) {
       const int v = (int)b.get(5);
@@ -400,43 +542,36 @@ __global__ void __launch_bounds__(XTC_DECODE_THREADS, 1)
     const uint32_t n_small = (uint32_t)run / 3u;
     if (i + 1u + n_small > natoms) return xtc_fail(err, XERR_ATOMS, f);
     if (n_small == 0) {
-      o.put(f, i, big, inv);
+      o.put(f, i, big, h.inv);
       ++i;
     } else {
       const uint32_t ss = (uint32_t)c_ranges[smallidx];
       const uint64_t ms = c_range_inv.v[smallidx];
       int32_t prev[3] = {big[0], big[1], big[2]};
       for (uint32_t k = 0; k < n_small; ++k) {
-        int32_t s[3];
-        get_triple(b, smallidx, ss, ms, ss, ms, s);
+        int32_t sv[3];
+        get_triple(b, smallidx, ss, ms, ss, ms, sv);
 #pragma unroll
-        for (int d = 0; d < 3; ++d) s[d] = wadd(wadd(s[d], prev[d]), -smallnum);
+        for (int d = 0; d < 3; ++d) sv[d] = wadd(wadd(sv[d], prev[d]), -smallnum);
         // the first small atom comes before the large one (the encoder
         // swapped the two: water-like groups compress better)
-        o.put(f, i, s, inv);
+        o.put(f, i, sv, h.inv);
         if (k == 0) {
-          o.put(f, i + 1, big, inv);
+          o.put(f, i + 1, big, h.inv);
           i += 2;
         } else {
           i += 1;
         }
 #pragma unroll
-        for (int d = 0; d < 3; ++d) prev[d] = s[d];
+        for (int d = 0; d < 3; ++d) prev[d] = sv[d];
       }
     }
     if (is_smaller != 0) {
       smallidx += is_smaller;
       if (smallidx < XTC_FIRST || smallidx >= XTC_LAST) return xtc_fail(err, XERR_INDEX, f);
-      if (is_smaller < 0) {
-        smallnum = smaller;
-        smaller = smallidx > XTC_FIRST ? c_ranges[smallidx - 1] / 2 : 0;
-      } else {
-        smaller = smallnum;
-        smallnum = c_ranges[smallidx] / 2;
-      }
+      smallnum = c_ranges[smallidx] / 2;  // as the reference's smaller/smallnum updates give
     }
   }
-  if (b.consumed_bits() > 8ull * n_bytes) xtc_fail(err, XERR_OVERRUN, f);
 }
 
 const char* xerr_text(uint32_t code) {
@@ -445,6 +580,7 @@ const char* xerr_text(uint32_t code) {
     case XERR_RANGE: return "empty or 32-bit coordinate range";
     case XERR_ATOMS: return "run of small atoms past the atom count";
     case XERR_OVERRUN: return "compressed bits past the byte count";
+    case XERR_BIG: return "compressed frame of 256 MB or more";
     default: return "malformed compressed frame";
   }
 }
@@ -743,7 +879,15 @@ int decode_to_device(Ctx& c, const char* path, const size_t* usecols, size_t n_u
   int32_t* d_map = map.empty() ? nullptr
                                : static_cast<int32_t*>(c.arena.alloc(4 * map.size()));
   uint32_t* d_xerr = static_cast<uint32_t*>(c.arena.alloc(16));
-  if (!d_file || !d_off || (!map.empty() && !d_map) || !d_xerr)
+  // decoding segments: a checkpoint per XTC_SEG_ATOMS atoms of every frame
+  const uint32_t max_seg = std::max<uint32_t>(1, (ix.natoms + XTC_SEG_ATOMS - 1) / XTC_SEG_ATOMS);
+  const uint64_t n_threads2 = (uint64_t)n_frames * max_seg;
+  if (n_threads2 > (uint64_t)UINT32_MAX * XTC_DECODE_THREADS)
+    return c.fail(ENT_ERR_TOO_LARGE, "trajectory too large for one call");
+  XtcCheckpoint* d_cp =
+      static_cast<XtcCheckpoint*>(c.arena.alloc(sizeof(XtcCheckpoint) * n_threads2));
+  uint32_t* d_nseg = static_cast<uint32_t*>(c.arena.alloc(4ull * n_frames));
+  if (!d_file || !d_off || (!map.empty() && !d_map) || !d_xerr || !d_cp || !d_nseg)
     return c.fail(ENT_ERR_CUDA, "out of device memory");
   s = upload_file(c, path, ix.end, d_file);
   if (s) return s;
@@ -756,9 +900,19 @@ int decode_to_device(Ctx& c, const char* path, const size_t* usecols, size_t n_u
   if (n_use == 0) return ENT_OK;
   DecodeOut o{d_out, col_stride, row_stride, d_map};
   cudaEventRecord(c.ev_k0, c.stream);
-  k_xtc_decode<<<(n_frames + XTC_DECODE_THREADS - 1) / XTC_DECODE_THREADS, XTC_DECODE_THREADS,
-                 0, c.stream>>>(d_file, d_off, n_frames, ix.natoms, o, d_xerr);
+  // one walk per warp while the frames fill fewer than 8 warps per SM
+  const uint32_t stride = (uint64_t)n_frames < 8ull * 32 * (uint64_t)c.n_sms ? 32u : 1u;
+  const uint64_t n_threads1 = (uint64_t)n_frames * stride;
+  k_xtc_walk<<<(unsigned)((n_threads1 + XTC_DECODE_THREADS - 1) / XTC_DECODE_THREADS),
+               XTC_DECODE_THREADS, 0, c.stream>>>(d_file, d_off, n_frames, ix.natoms, max_seg,
+                                                  stride, d_cp, d_nseg, d_xerr);
   e = cudaGetLastError();
+  if (e == cudaSuccess) {
+    k_xtc_decode<<<(unsigned)((n_threads2 + XTC_DECODE_THREADS - 1) / XTC_DECODE_THREADS),
+                   XTC_DECODE_THREADS, 0, c.stream>>>(d_file, d_off, n_frames, ix.natoms, max_seg,
+                                                      d_cp, d_nseg, o, d_xerr);
+    e = cudaGetLastError();
+  }
   if (e != cudaSuccess) return c.cuda_fail(e, "decode launch");
   cudaEventRecord(c.ev_k1, c.stream);
   uint32_t herr[2] = {0, 0};
@@ -768,7 +922,7 @@ int decode_to_device(Ctx& c, const char* path, const size_t* usecols, size_t n_u
   if (herr[0] != XERR_NONE)
     return c.fail(ENT_ERR_IO, std::string(path) + ": frame " + std::to_string(herr[1]) + ": " +
                                   xerr_text(herr[0]));
-  c.stats.kernel_launches = 1;
+  c.stats.kernel_launches = 2;
   c.stats.instances = n_frames;
   return ENT_OK;
 }

@@ -332,9 +332,10 @@ const char* ent_io_last_error(void);
 int ent_xtc_file_shape(const char* path, size_t* n_frames, size_t* n_cols);
 /* Decode the file on the device into the column-major n_rows x n_cols_out
  * matrix d_out (device memory of ctx's device): the file is indexed on the
- * host, copied to the device through pinned buffers and decoded by one
- * thread per frame. usecols as for ent_read_coords (the file's column
- * order). A malformed compressed frame is ENT_ERR_IO naming the frame. */
+ * host, copied to the device through pinned buffers, walked once per frame
+ * (atom-group positions) and decoded by one thread per 64-atom segment.
+ * usecols as for ent_read_coords (the file's column order). A malformed
+ * compressed frame is ENT_ERR_IO naming the frame. */
 int ent_load_xtc_device(ent_ctx* ctx, const char* path, const size_t* usecols,
                         size_t n_usecols, float* d_out, size_t n_rows, size_t n_cols_out);
 /* Same into host memory: primary_index 'C' column-major, 'R' row-major (the
