@@ -366,7 +366,15 @@ __device__ __forceinline__ uint32_t be_word(const uint32_t* p) {
 }
 
 // Header of frame f (natoms > 9); false (and err set) for a malformed one.
-__device__ bool parse_head(const uint32_t* fw, uint32_t f, FrameHead& h, uint32_t* err) {
+// file_end: one past the uploaded file's last word. The host's index already
+// keeps every frame inside the file; the checks here keep the kernels inside
+// the buffer even if the file changed between the index and the copy.
+__device__ bool parse_head(const uint32_t* fw, uint32_t f, FrameHead& h, uint32_t* err,
+                           const uint32_t* file_end) {
+  if (fw + 23 > file_end) {
+    xtc_fail(err, XERR_OVERRUN, f);
+    return false;
+  }
   const float precision = __uint_as_float(be_word(fw + 14));
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
@@ -377,6 +385,7 @@ __device__ bool parse_head(const uint32_t* fw, uint32_t f, FrameHead& h, uint32_
   h.n_bytes = be_word(fw + 22);
   h.data = fw + 23;
   h.dend = h.data + ((h.n_bytes + 3u) >> 2);
+  if (h.dend > file_end || h.dend < h.data) h.dend = file_end;
   if (h.smallidx < XTC_FIRST || h.smallidx >= XTC_LAST) {
     xtc_fail(err, XERR_INDEX, f);
     return false;
@@ -426,7 +435,8 @@ __device__ bool parse_head(const uint32_t* fw, uint32_t f, FrameHead& h, uint32_
 __global__ void __launch_bounds__(XTC_DECODE_THREADS)
     k_xtc_walk(const uint8_t* __restrict__ file, const uint64_t* __restrict__ frame_off,
                uint32_t n_frames, uint32_t natoms, uint32_t max_seg, uint32_t stride,
-               XtcCheckpoint* __restrict__ cps, uint32_t* __restrict__ n_seg, uint32_t* err) {
+               const uint32_t* file_end, XtcCheckpoint* __restrict__ cps,
+               uint32_t* __restrict__ n_seg, uint32_t* err) {
   const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (tid % stride) return;
   const uint64_t fl = tid / stride;
@@ -435,13 +445,15 @@ __global__ void __launch_bounds__(XTC_DECODE_THREADS)
   n_seg[f] = 0;
   XtcCheckpoint* cp = cps + (size_t)f * max_seg;
   if (natoms <= 9) {  // raw floats: one segment
+    const uint32_t* fw = reinterpret_cast<const uint32_t*>(file + frame_off[f]);
+    if (fw + 14 + 3 * natoms > file_end) return xtc_fail(err, XERR_OVERRUN, f);
     cp[0] = XtcCheckpoint{0, 0, 0, 0};
     n_seg[f] = 1;
     return;
   }
   const uint32_t* fw = reinterpret_cast<const uint32_t*>(file + frame_off[f]);
   FrameHead h;
-  if (!parse_head(fw, f, h, err)) return;
+  if (!parse_head(fw, f, h, err, file_end)) return;
   const uint32_t big_bits =
       h.large ? (uint32_t)(h.bits_d[0] + h.bits_d[1] + h.bits_d[2]) : (uint32_t)h.bitsize;
   const uint32_t n_words = (uint32_t)(h.dend - h.data);
@@ -494,8 +506,8 @@ __global__ void __launch_bounds__(XTC_DECODE_THREADS)
 __global__ void __launch_bounds__(XTC_DECODE_THREADS)
     k_xtc_decode(const uint8_t* __restrict__ file, const uint64_t* __restrict__ frame_off,
                  uint32_t n_frames, uint32_t natoms, uint32_t max_seg,
-                 const XtcCheckpoint* __restrict__ cps, const uint32_t* __restrict__ n_seg,
-                 DecodeOut o, uint32_t* err) {
+                 const uint32_t* file_end, const XtcCheckpoint* __restrict__ cps,
+                 const uint32_t* __restrict__ n_seg, DecodeOut o, uint32_t* err) {
   const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (uint64_t)n_frames * max_seg) return;
   const uint32_t f = (uint32_t)(t % n_frames), seg = (uint32_t)(t / n_frames);
@@ -514,7 +526,7 @@ __global__ void __launch_bounds__(XTC_DECODE_THREADS)
     return;
   }
   FrameHead h;
-  if (!parse_head(fw, f, h, err)) return;
+  if (!parse_head(fw, f, h, err, file_end)) return;
   const XtcCheckpoint cp = cps[(size_t)f * max_seg + seg];
   const uint32_t end = seg + 1 < ns ? cps[(size_t)f * max_seg + seg + 1].atom : natoms;
   BitReader b;
@@ -899,18 +911,19 @@ int decode_to_device(Ctx& c, const char* path, const size_t* usecols, size_t n_u
   if (e != cudaSuccess) return c.cuda_fail(e, "copy frame index");
   if (n_use == 0) return ENT_OK;
   DecodeOut o{d_out, col_stride, row_stride, d_map};
+  const uint32_t* file_end = reinterpret_cast<const uint32_t*>(d_file + (ix.end & ~3ull));
   cudaEventRecord(c.ev_k0, c.stream);
   // one walk per warp while the frames fill fewer than 8 warps per SM
   const uint32_t stride = (uint64_t)n_frames < 8ull * 32 * (uint64_t)c.n_sms ? 32u : 1u;
   const uint64_t n_threads1 = (uint64_t)n_frames * stride;
   k_xtc_walk<<<(unsigned)((n_threads1 + XTC_DECODE_THREADS - 1) / XTC_DECODE_THREADS),
                XTC_DECODE_THREADS, 0, c.stream>>>(d_file, d_off, n_frames, ix.natoms, max_seg,
-                                                  stride, d_cp, d_nseg, d_xerr);
+                                                  stride, file_end, d_cp, d_nseg, d_xerr);
   e = cudaGetLastError();
   if (e == cudaSuccess) {
     k_xtc_decode<<<(unsigned)((n_threads2 + XTC_DECODE_THREADS - 1) / XTC_DECODE_THREADS),
                    XTC_DECODE_THREADS, 0, c.stream>>>(d_file, d_off, n_frames, ix.natoms, max_seg,
-                                                      d_cp, d_nseg, o, d_xerr);
+                                                      file_end, d_cp, d_nseg, o, d_xerr);
     e = cudaGetLastError();
   }
   if (e != cudaSuccess) return c.cuda_fail(e, "decode launch");
