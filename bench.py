@@ -720,7 +720,8 @@ def xtc_config(ctx, n_atoms: int = 1000, n_frames: int = 50_000):
         "load_device_s": wall, "load_device_MB_per_s": size / wall / 1e6,
         "coordinates_per_s": 3 * n_atoms * n_frames / wall,
         "decode_kernel_ms": k_ms, "index_s": t_index,
-        "decode_roofline": {"bound": "latency (one serial bit stream per thread)",
+        "decode_roofline": {"bound": "latency (a dependent walk per frame over its atom "
+                                     "groups, then one thread per 64-atom segment)",
                             "algorithmic_bytes": size + out_bytes,
                             "achieved_gbs": (size + out_bytes) / (k_ms / 1e3) / 1e9,
                             "peak_gbs": peak, "frac": (size + out_bytes) / (k_ms / 1e3) / 1e9 / peak,
