@@ -74,6 +74,9 @@ def parse():
                          "own")
     ap.add_argument("--xtc-atoms", type=int, default=1000,
                     help="atoms of the --xtc-frames trajectory (default 1000)")
+    ap.add_argument("--coords-file", action="store_true",
+                    help="time only the ASCII coordinate-file reader and device loader on the "
+                         "64 x 100k MI matrix; prints a JSON line of its own")
     ap.add_argument("--coords", type=int, default=N_COORDS,
                     help="coordinates of the MI batch (64 = the benchmark workload; "
                          "smaller values give the small case used for ncu captures)")
@@ -617,31 +620,45 @@ def other_configs(ctx):
     ref["dens_D3_16x100k"] = {"ms": st.total_ms, "densities": int(d3.shape[0]),
                               "d2h_bytes": int(d3.nbytes)}
     out["reference_formulas"] = ref
-    # the reference's ASCII coordinate format: parallel host parse, and the
-    # device loader with pinned, overlapped copies
+    out["coords_file_64x100k"] = coords_file_config(ctx, xm)
+    out["xtc_1000atoms_50k"] = xtc_config(ctx)
+    return out
+
+
+def coords_file_config(ctx, xm: np.ndarray, reps: int = 3) -> dict:
+    """The reference's ASCII coordinate format (Tools::IO::read_coords,
+    tools.hxx:153-235) for the MI matrix, written with 9 significant digits
+    (which give every float back exactly): the parallel host parse (shape,
+    then values, as the reference's two passes), and the device loader with
+    pinned, overlapped copies. Best of `reps` calls each, the file in the
+    page cache."""
     import tempfile
     import torch
     from entropical_gb300 import read_coords
     with tempfile.TemporaryDirectory() as td:
         path = os.path.join(td, "coords.txt")
-        np.savetxt(path, xm.T, fmt="%.8g")
+        np.savetxt(path, xm.T, fmt="%.9g")
         size = os.path.getsize(path)
-        t0 = time.perf_counter()
-        host = read_coords(path)
-        t_host = time.perf_counter() - t0
+        t_host, t_dev = [], []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            host = read_coords(path)
+            t_host.append(time.perf_counter() - t0)
         dev = torch.empty(host.shape, dtype=torch.float32, device="cuda")
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        ctx.load_coords_device(path, dev.data_ptr())
-        torch.cuda.synchronize()
-        t_dev = time.perf_counter() - t0
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            ctx.load_coords_device(path, dev.data_ptr())
+            torch.cuda.synchronize()
+            t_dev.append(time.perf_counter() - t0)
         same = bool(torch.equal(dev.cpu(), torch.from_numpy(host)))
-    out["coords_file_64x100k"] = {"bytes": size, "read_s": t_host,
-                                  "read_MB_per_s": size / t_host / 1e6, "load_device_s": t_dev,
-                                  "load_device_MB_per_s": size / t_dev / 1e6,
-                                  "device_equals_host": same, "threads": os.cpu_count()}
-    out["xtc_1000atoms_50k"] = xtc_config(ctx)
-    return out
+        exact = bool(np.array_equal(host, xm.astype(np.float32)))
+    t_h, t_d = min(t_host), min(t_dev)
+    return {"bytes": size, "values": int(xm.size), "read_s": t_h,
+            "read_MB_per_s": size / t_h / 1e6, "load_device_s": t_d,
+            "load_device_MB_per_s": size / t_d / 1e6, "reps": reps,
+            "device_equals_host": same, "host_equals_values_written": exact,
+            "threads": os.cpu_count()}
 
 
 def xtc_trajectory(n_atoms: int, n_frames: int, seed: int = 21) -> np.ndarray:
@@ -823,6 +840,11 @@ def main():
     if args.xtc_frames:
         from entropical_gb300 import Context
         print(json.dumps(xtc_config(Context(), n_atoms=args.xtc_atoms, n_frames=args.xtc_frames)))
+        return None
+    if args.coords_file:
+        from entropical_gb300 import Context, workloads
+        xm = workloads.mi_coords(N_FRAMES, N_COORDS, seed=2024)
+        print(json.dumps(coords_file_config(Context(), xm)))
         return None
     ws, rank, local = dist_env()
     from entropical_gb300 import workloads

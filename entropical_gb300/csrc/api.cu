@@ -122,6 +122,7 @@ int Ctx::ensure_staging(size_t bytes) {
     if (e == cudaSuccess && !ev_stage[k])
       e = cudaEventCreateWithFlags(&ev_stage[k], cudaEventDisableTiming);
     if (e != cudaSuccess) {
+      if (h_stage[k]) cudaFreeHost(h_stage[k]);
       h_stage[k] = nullptr;
       return cuda_fail(e, "pinned staging");
     }

@@ -4,23 +4,30 @@
 // text matrix with a two-pass std::ifstream parser: the first non-empty line
 // gives n_cols, the number of non-empty lines gives n_rows, then every value
 // is read with `ifs >> float` into a row-major ('R') or column-major ('C')
-// buffer, keeping only the requested columns. Here the file is read once into
-// memory, the starts of the non-empty lines are found by all host threads,
-// and rows are parsed in parallel with std::from_chars (correctly rounded,
-// like the strtof behind `ifs >> float`). ent_load_coords_device parses
-// blocks of rows into pinned staging buffers and copies each block to its
-// place in a column-major device matrix with one 2-D copy while the next
-// block is being parsed.
+// buffer, keeping only the requested columns. Here a regular file is mapped
+// read-only (other files are read into memory), the starts of the non-empty
+// lines are found by all host threads, and rows are parsed in parallel with
+// std::from_chars (correctly rounded, like the strtof behind `ifs >> float`).
+// ent_load_coords_device parses blocks of rows into pinned staging buffers
+// and copies each block to its place in a column-major device matrix with one
+// 2-D copy while the next block is being parsed.
 //
 // Differences from the reference, all on malformed input: a row with a
 // different number of values than the first is an error (the reference reads
 // values across line ends and silently shifts the matrix); a value that is
-// not a number is an error (the reference leaves it unread). A leading '+'
-// is accepted, as `ifs >> float` does.
+// not a number is an error (the reference leaves it unread); a value above
+// the float range is +-infinity, as strtof gives it (the reference stores
+// +-FLT_MAX there and reads nothing after it: every later value of the matrix
+// repeats it). A leading '+' is accepted, as `ifs >> float` does.
 #include <cuda_runtime.h>
+#include <fcntl.h>
+#include <sys/mman.h>
+#include <sys/stat.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <atomic>
+#include <cerrno>
 #include <charconv>
 #include <cmath>
 #include <cstdio>
@@ -34,12 +41,26 @@
 
 namespace {
 
+// The file's bytes: a read-only mapping of a regular file (no copy; the
+// pages are faulted in by the threads that scan them), else the whole stream
+// read into memory (pipes, files that cannot be mapped). As with any mapped
+// reader, a file truncated by another process while it is being read ends
+// this one with SIGBUS.
 struct TextFile {
-  std::vector<char> buf;
+  const char* data = nullptr;
+  size_t size = 0;
+  void* map = nullptr;
+  std::vector<char> owned;
   std::vector<size_t> line_start;  // non-empty lines
   std::vector<size_t> line_end;
   size_t n_cols = 0;
   std::string error;
+  TextFile() = default;
+  TextFile(const TextFile&) = delete;
+  TextFile& operator=(const TextFile&) = delete;
+  ~TextFile() {
+    if (map) munmap(map, size);
+  }
 };
 
 unsigned n_threads() {
@@ -64,34 +85,48 @@ void parallel_for(size_t n, F f) {
 
 inline bool is_space(char c) { return c == ' ' || c == '\t' || c == '\r' || c == '\v' || c == '\f'; }
 
-// Reads the file and indexes its non-empty lines (a line of spaces counts, as
-// a non-empty std::getline result does in the reference).
+// Maps (or reads) the file and indexes its non-empty lines (a line of spaces
+// counts, as a non-empty std::getline result does in the reference; a last
+// line without a line break counts too).
 bool load_text(const char* path, TextFile* tf) {
-  FILE* f = std::fopen(path, "rb");
-  if (!f) {
+  const int fd = open(path, O_RDONLY | O_CLOEXEC);
+  if (fd < 0) {
     tf->error = std::string("cannot open ") + path;
     return false;
   }
-  std::fseek(f, 0, SEEK_END);
-  const long sz = std::ftell(f);
-  std::fseek(f, 0, SEEK_SET);
-  if (sz < 0) {
-    std::fclose(f);
-    tf->error = "cannot size file";
-    return false;
+  struct stat st;
+  const bool regular = fstat(fd, &st) == 0 && S_ISREG(st.st_mode);
+  if (regular && st.st_size > 0) {
+    void* m = mmap(nullptr, (size_t)st.st_size, PROT_READ, MAP_PRIVATE, fd, 0);
+    if (m != MAP_FAILED) {
+      tf->map = m;
+      tf->data = static_cast<const char*>(m);
+      tf->size = (size_t)st.st_size;
+    }
   }
-  tf->buf.resize((size_t)sz + 1);
-  const size_t got = sz ? std::fread(tf->buf.data(), 1, (size_t)sz, f) : 0;
-  std::fclose(f);
-  if (got != (size_t)sz) {
-    tf->error = "short read";
-    return false;
+  if (!tf->map) {  // also files that report no size (procfs)
+    size_t got = 0;
+    tf->owned.resize(std::max<size_t>(regular ? (size_t)st.st_size : 0, (size_t)1 << 16));
+    while (true) {
+      if (got == tf->owned.size()) tf->owned.resize(2 * got);
+      const ssize_t r = read(fd, tf->owned.data() + got, tf->owned.size() - got);
+      if (r < 0 && errno == EINTR) continue;
+      if (r < 0) {
+        close(fd);
+        tf->error = std::string("cannot read ") + path;
+        return false;
+      }
+      if (r == 0) break;
+      got += (size_t)r;
+    }
+    tf->data = tf->owned.data();
+    tf->size = got;
   }
-  tf->buf[(size_t)sz] = '\n';
-  const char* b = tf->buf.data();
-  const size_t n = (size_t)sz;
+  close(fd);
+  const char* b = tf->data;
+  const size_t n = tf->size;
   // per-thread line scan over byte ranges split at line ends
-  const unsigned T = n_threads();
+  const unsigned T = (unsigned)std::min<size_t>(n_threads(), std::max<size_t>(1, n >> 16));
   std::vector<size_t> cut(T + 1, 0);
   cut[T] = n;
   for (unsigned t = 1; t < T; ++t) {
@@ -104,8 +139,8 @@ bool load_text(const char* path, TextFile* tf) {
     for (size_t t = a; t < bb; ++t) {
       size_t p = cut[t];
       while (p < cut[t + 1]) {
-        const char* q = static_cast<const char*>(std::memchr(b + p, '\n', n + 1 - p));
-        const size_t end = (size_t)(q - b);
+        const char* q = static_cast<const char*>(std::memchr(b + p, '\n', cut[t + 1] - p));
+        const size_t end = q ? (size_t)(q - b) : cut[t + 1];
         if (end > p) {
           s[t].push_back(p);
           e[t].push_back(end);
@@ -131,12 +166,43 @@ bool load_text(const char* path, TextFile* tf) {
   return true;
 }
 
+// Whether a decimal token that does not fit a float lies below its range
+// (else above it): the power of ten of its first nonzero digit, the explicit
+// exponent included, is negative ("0.000...1" as well as "1e-50").
+bool below_float_range(const char* p, const char* end) {
+  if (p < end && *p == '-') ++p;
+  long int_sig = 0, frac_zeros = 0;  // integer digits from the first nonzero; zeros after '.'
+  bool dot = false, nz = false;
+  for (; p < end && *p != 'e' && *p != 'E'; ++p) {
+    if (*p == '.') {
+      dot = true;
+    } else if (!dot) {
+      nz = nz || *p != '0';
+      int_sig += nz;
+    } else if (!nz) {
+      if (*p != '0') break;
+      ++frac_zeros;
+    }
+  }
+  long e10 = int_sig > 0 ? int_sig - 1 : -(frac_zeros + 1);
+  while (p < end && *p != 'e' && *p != 'E') ++p;
+  if (p < end) {  // the explicit exponent, saturated
+    ++p;
+    const bool eneg = p < end && *p == '-';
+    if (p < end && (*p == '-' || *p == '+')) ++p;
+    long ev = 0;
+    for (; p < end && *p >= '0' && *p <= '9'; ++p) ev = std::min(10 * ev + (*p - '0'), 1000000L);
+    e10 += eneg ? -ev : ev;
+  }
+  return e10 < 0;
+}
+
 // Parses rows [r0, r1) into dst: element (row r, used column u) at
 // dst[u * col_stride + (r - r0) * row_stride]. Returns false on a malformed
 // row (message in err).
 bool parse_rows(const TextFile& tf, size_t r0, size_t r1, const std::vector<int>& use,
                 float* dst, size_t col_stride, size_t row_stride, std::string* err) {
-  const char* b = tf.buf.data();
+  const char* b = tf.data;
   const size_t nc = tf.n_cols;
   for (size_t r = r0; r < r1; ++r) {
     const char* p = b + tf.line_start[r];
@@ -160,12 +226,7 @@ bool parse_rows(const TextFile& tf, size_t r0, size_t r1, const std::vector<int>
       // out-of-range values saturate as strtof does
       if (res.ec == std::errc::result_out_of_range) {
         const bool neg = *tok == '-';
-        bool tiny = false;
-        for (const char* z = tok; z < res.ptr; ++z)
-          if (*z == 'e' || *z == 'E') {
-            tiny = z[1] == '-';
-            break;
-          }
+        const bool tiny = below_float_range(tok, res.ptr);
         v = tiny ? (neg ? -0.f : 0.f) : (neg ? -HUGE_VALF : HUGE_VALF);
       }
       if (use[c] >= 0) dst[(size_t)use[c] * col_stride + (r - r0) * row_stride] = v;
@@ -293,41 +354,35 @@ int ent_load_coords_device(ent_ctx* ctx, const char* path, const size_t* usecols
   }
   if (n_rows == 0 || nu == 0) return ENT_OK;
   if (cudaSetDevice(c.device) != cudaSuccess) return c.cuda_fail(cudaGetLastError(), "set device");
-  // blocks of rows, double-buffered pinned staging (column-major per block)
-  const size_t R = std::min<size_t>(n_rows, std::max<size_t>(4096, (size_t)(8u << 20) / (4 * nu)));
-  float* stage[2] = {nullptr, nullptr};
-  cudaEvent_t done[2] = {nullptr, nullptr};
-  int rc = ENT_OK;
-  for (int i = 0; i < 2 && rc == ENT_OK; ++i) {
-    if (cudaHostAlloc(reinterpret_cast<void**>(&stage[i]), 4 * R * nu, cudaHostAllocDefault) !=
-            cudaSuccess ||
-        cudaEventCreateWithFlags(&done[i], cudaEventDisableTiming) != cudaSuccess)
-      rc = c.cuda_fail(cudaGetLastError(), "pinned staging");
-  }
+  // blocks of rows (8 MB, at least one row) through the context's two pinned
+  // staging buffers, column-major per block, one parsed while the other is
+  // being copied
+  const size_t row_bytes = 4 * nu;
+  const size_t blk_bytes = std::max(row_bytes, std::min(row_bytes * n_rows, (size_t)8 << 20));
+  int rc = c.ensure_staging(blk_bytes);
+  if (rc) return rc;
+  const size_t R = std::min(n_rows, blk_bytes / row_bytes);
   size_t blk = 0;
   for (size_t r0 = 0; rc == ENT_OK && r0 < n_rows; r0 += R, ++blk) {
     const size_t r1 = std::min(n_rows, r0 + R), nr = r1 - r0;
     const int b = (int)(blk & 1);
-    if (blk >= 2 && cudaEventSynchronize(done[b]) != cudaSuccess) {
+    float* stage = reinterpret_cast<float*>(c.h_stage[b]);
+    if (blk >= 2 && cudaEventSynchronize(c.ev_stage[b]) != cudaSuccess) {
       rc = c.cuda_fail(cudaGetLastError(), "staging reuse");
       break;
     }
-    if (!parallel_parse(tf, r0, r1, use, stage[b], nr, 1, &g_io_error)) {
+    if (!parallel_parse(tf, r0, r1, use, stage, nr, 1, &g_io_error)) {
       rc = c.fail(ENT_ERR_IO, g_io_error);
       break;
     }
     // nu columns of nr values into the column-major n_rows x nu matrix
-    cudaError_t e = cudaMemcpy2DAsync(d_out + r0, 4 * n_rows, stage[b], 4 * nr, 4 * nr, nu,
+    cudaError_t e = cudaMemcpy2DAsync(d_out + r0, 4 * n_rows, stage, 4 * nr, 4 * nr, nu,
                                       cudaMemcpyHostToDevice, c.stream);
-    if (e == cudaSuccess) e = cudaEventRecord(done[b], c.stream);
+    if (e == cudaSuccess) e = cudaEventRecord(c.ev_stage[b], c.stream);
     if (e != cudaSuccess) rc = c.cuda_fail(e, "copy block");
   }
   if (cudaStreamSynchronize(c.stream) != cudaSuccess && rc == ENT_OK)
     rc = c.cuda_fail(cudaGetLastError(), "copy");
-  for (int i = 0; i < 2; ++i) {
-    if (stage[i]) cudaFreeHost(stage[i]);
-    if (done[i]) cudaEventDestroy(done[i]);
-  }
   return rc;
 }
 

@@ -90,3 +90,62 @@ def test_large_file_parallel_parse(tmp_path):
     y = read_coords(p)
     assert np.array_equal(y, x)
     assert os.path.getsize(p) > 4_000_000
+
+
+def test_empty_and_blank_files(tmp_path):
+    assert coords_file_shape(write(tmp_path / "e.txt", "")) == (0, 0)
+    assert coords_file_shape(write(tmp_path / "b.txt", "\n\n\n")) == (0, 0)
+    assert read_coords(str(tmp_path / "e.txt")).shape == (0, 0)
+
+
+def test_large_file_ragged_layout(tmp_path):
+    """Many threads' byte ranges over CRLF lines, runs of blank lines and a
+    last line without a line break: the same rows as the values written."""
+    rng = np.random.default_rng(11)
+    x = rng.standard_normal((4, 60_000)).astype(np.float32)
+    rows = [" ".join("%.9g" % v for v in r) for r in x.T]
+    parts = []
+    for i, r in enumerate(rows):
+        parts.append(r)
+        parts.append("\r\n" + ("\n" * int(i % 97 == 0)))
+    text = "".join(parts).rstrip("\r\n")  # no final line break
+    p = write(tmp_path / "big.txt", text)
+    assert coords_file_shape(p) == (60_000, 4)
+    assert np.array_equal(read_coords(p), x)
+    assert np.array_equal(read_coords(p, usecols=[2], primary="R")[:, 0], x[2])
+
+
+def test_stream_without_size(tmp_path):
+    """A file that cannot be mapped (a FIFO) is read as a stream."""
+    import threading
+    fifo = tmp_path / "c.fifo"
+    os.mkfifo(fifo)
+    text = "".join(f"{i} {i + 0.5} {-i}\n" for i in range(50_000))
+
+    def writer():
+        with open(fifo, "w") as f:
+            f.write(text)
+
+    th = threading.Thread(target=writer, daemon=True)
+    th.start()
+    assert coords_file_shape(str(fifo)) == (50_000, 3)
+    th.join(timeout=30)
+    assert not th.is_alive()
+
+
+def test_values_beyond_float_range(tmp_path):
+    """Values below the float range read as (signed) zero or the subnormal
+    strtof gives, however they are spelled; the reference's `ifs >> float`
+    reads the same. Values above it saturate to infinity as strtof does (the
+    reference stores FLT_MAX there and reads nothing after it)."""
+    z50 = "0." + "0" * 50 + "1"
+    p = write(tmp_path / "tiny.txt", f"{z50} -{z50} 1e-50 -1e-50\n.00001e-45 1e-40 8e-46 0.5\n")
+    y = read_coords(p, primary="R")
+    assert np.array_equal(y.view(np.uint32), np.array(
+        [[0.0, -0.0, 0.0, -0.0], [0.0, np.float32(1e-40), np.float32(1.4e-45), 0.5]],
+        np.float32).view(np.uint32))
+    if HAVE_REF:
+        assert np.array_equal(y.view(np.uint32), O.ref_read_coords(p, "R").view(np.uint32))
+    p = write(tmp_path / "huge.txt", "1e39 -1e39 " + "9" * 42 + " 0.0001e50\n")
+    assert np.array_equal(read_coords(p, primary="R"),
+                          np.array([[np.inf, -np.inf, np.inf, np.inf]], np.float32))

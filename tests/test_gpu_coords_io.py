@@ -9,11 +9,12 @@ from entropical_gb300 import read_coords
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("usecols", [None, [0, 5, 63]])
-def test_device_loader_matches_host(ctx, tmp_path, usecols):
+@pytest.mark.parametrize("usecols,n", [(None, 40_000), ([0, 5, 63], 40_000), (None, 110_000)])
+def test_device_loader_matches_host(ctx, tmp_path, usecols, n):
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(11)
-    x = rng.standard_normal((64, 40_000)).astype(np.float32)  # 2 blocks of rows
+    # 8 MB blocks of rows: 2 blocks, 1 block, 4 blocks (both staging buffers reused)
+    x = rng.standard_normal((64, n)).astype(np.float32)
     p = str(tmp_path / "c.txt")
     np.savetxt(p, x.T, fmt="%.8g")
     host = read_coords(p, usecols)
