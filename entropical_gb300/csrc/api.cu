@@ -36,6 +36,7 @@ void* Arena::alloc(size_t bytes) {
     void* p = static_cast<char*>(blocks.back().ptr) + used_in_last;
     used_in_last += bytes;
     total_used += bytes;
+    peak = std::max(peak, total_used);
     return p;
   }
   size_t sz = std::max(bytes, blocks.empty() ? (size_t)64 << 20
@@ -52,12 +53,13 @@ void* Arena::alloc(size_t bytes) {
   blocks.push_back({p, sz});
   used_in_last = bytes;
   total_used += bytes;
+  peak = std::max(peak, total_used);
   return p;
 }
 
 void Arena::coalesce() {
   if (blocks.size() > 1) {
-    size_t want = std::max(total_used, (size_t)64 << 20);
+    size_t want = std::max(peak, (size_t)64 << 20);
     for (auto& b : blocks) cudaFree(b.ptr);
     blocks.clear();
     void* p = nullptr;
@@ -70,18 +72,30 @@ void Arena::reset() {
   coalesce();
   used_in_last = 0;
   total_used = 0;
+  peak = 0;
 }
 
-size_t Arena::spare() const {
-  size_t cap = 0;
-  for (const auto& b : blocks) cap += b.size;
-  return cap > total_used ? cap - total_used : 0;
+// Allocations come from the last block only (the tails of earlier ones stay
+// unused until the blocks are coalesced).
+size_t Arena::spare() const { return blocks.empty() ? 0 : blocks.back().size - used_in_last; }
+
+void Arena::rewind(const Mark& m) {
+  if (blocks.size() > m.n_blocks) {
+    const Block last = blocks.back();
+    for (size_t i = m.n_blocks; i + 1 < blocks.size(); ++i) cudaFree(blocks[i].ptr);
+    blocks.resize(m.n_blocks);
+    blocks.push_back(last);
+    used_in_last = 0;
+  } else {
+    used_in_last = m.used_in_last;
+  }
+  total_used = m.total_used;
 }
 
 void Arena::release() {
   for (auto& b : blocks) cudaFree(b.ptr);
   blocks.clear();
-  used_in_last = total_used = 0;
+  used_in_last = total_used = peak = 0;
 }
 
 // ---------------------------------------------------------------- context
@@ -306,7 +320,7 @@ int sort_views(Ctx& c, const std::vector<ViewSpec>& views, SortedViews* out) {
 }
 
 int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
-                std::vector<InstSpec>& insts, uint32_t mode, EngineOut* out) {
+                const std::vector<InstSpec>& insts, uint32_t mode, EngineOut* out) {
   cudaError_t e;
   const cudaStream_t st = c.stream;
   const uint32_t nv = (uint32_t)views.size();
@@ -409,7 +423,7 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
   for (int d = 1; d <= 3; ++d) {
     group_base[d] = slot;
     for (uint32_t i : order) {
-      InstSpec& s = insts[i];
+      const InstSpec& s = insts[i];
       if ((int)s.d != d) continue;
       InstDev& I = hi[i];
       std::memset(&I, 0, sizeof(I));
@@ -763,6 +777,7 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
       }
     }
     rec(c.ev_k1);
+    c.ran_k = true;
     if (mode & (DM_LOGSUM | DM_SUMV)) {
       if ((r = launch_inst_logsum(st, di_sorted, ni, tile_ls, dls)) != cudaSuccess) return r;
       launches += 1;
@@ -819,6 +834,104 @@ int Engine::run(Ctx& c, const std::vector<ViewSpec>& views,
   return ENT_OK;
 }
 
+namespace {
+
+// Device bytes an engine run takes per point of an instance (sorted points,
+// strip order and its sort buffers, FP64 sums, the 1-D range and 2-D moment
+// prefix rows) and per point of a sorted view, rounded up from the MI and TE
+// batches' workspace (174 B per 2-D point with the moment rows, under 64 B
+// per 1-D or 3-D point), plus the per-instance tables.
+constexpr size_t kBatchBytesPerPoint[4] = {0, 64, 192, 64};
+constexpr size_t kBatchBytesPerViewPoint = 16;
+constexpr size_t kBatchBytesPerInstance = 4096;
+constexpr size_t kBatchMaxViews = 65535;
+
+size_t inst_bytes(const InstSpec& s) {
+  return (size_t)s.n * kBatchBytesPerPoint[std::min(s.d, 3u)] + kBatchBytesPerInstance;
+}
+
+// What an engine run may take: the device's free memory and the workspace
+// already held, less an eighth (at least 2 GB) for the allocator's rounding,
+// graphs and other work on the device.
+size_t batch_budget(Ctx& c) {
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+    cudaGetLastError();
+    free_b = 0;
+  }
+  const size_t avail = free_b + c.arena.spare();
+  const size_t reserve = std::max(avail / 8, (size_t)2 << 30);
+  return avail > reserve ? avail - reserve : avail / 2;
+}
+
+}  // namespace
+
+int run_engine_batches(Ctx& c, const std::vector<ViewSpec>& views,
+                       const std::vector<InstSpec>& insts, uint32_t mode, BatchDone done,
+                       void* arg) {
+  if (insts.empty()) return ENT_OK;
+  size_t est = 0;
+  for (const auto& q : insts) est += inst_bytes(q);
+  for (const auto& v : views) est += (size_t)v.n * kBatchBytesPerViewPoint;
+  const bool one_run = insts.size() <= c.max_batch_instances && views.size() <= kBatchMaxViews;
+  size_t budget = SIZE_MAX;
+  if (!one_run || est > c.arena.spare()) budget = batch_budget(c);
+  if (one_run && est <= budget) {
+    Engine eng;
+    EngineOut eo;
+    int s = eng.run(c, views, insts, mode, &eo);
+    if (s) return s;
+    return done ? done(arg, 0, insts.size(), eo) : ENT_OK;
+  }
+  // consecutive runs of as many instances as fit (at least one)
+  const Arena::Mark base = c.arena.mark();
+  std::vector<uint32_t> remap(views.size(), UINT32_MAX);
+  for (size_t q0 = 0; q0 < insts.size();) {
+    std::vector<ViewSpec> cv;
+    std::vector<InstSpec> ci;
+    std::vector<uint32_t> used;  // views mapped for this run
+    size_t bytes = 0, q = q0;
+    for (; q < insts.size(); ++q) {
+      InstSpec I = insts[q];
+      size_t add = inst_bytes(I), new_views = 0;
+      for (uint32_t j = 0; j < I.d; ++j) {
+        bool seen = remap[I.view[j]] != UINT32_MAX;
+        for (uint32_t k = 0; k < j; ++k) seen = seen || I.view[k] == I.view[j];
+        if (!seen) {
+          ++new_views;
+          add += (size_t)views[I.view[j]].n * kBatchBytesPerViewPoint;
+        }
+      }
+      if (q > q0 && (bytes + add > budget || ci.size() + 1 > c.max_batch_instances ||
+                     cv.size() + new_views > kBatchMaxViews))
+        break;
+      for (uint32_t j = 0; j < I.d; ++j) {
+        uint32_t& r = remap[I.view[j]];
+        if (r == UINT32_MAX) {
+          r = (uint32_t)cv.size();
+          cv.push_back(views[I.view[j]]);
+          used.push_back(I.view[j]);
+        }
+        I.view[j] = r;
+      }
+      ci.push_back(I);
+      bytes += add;
+    }
+    Engine eng;
+    EngineOut eo;
+    int s = eng.run(c, cv, ci, mode, &eo);
+    if (s == ENT_OK && done) s = done(arg, q0, ci.size(), eo);
+    if (s) return s;
+    cudaError_t e = cudaStreamSynchronize(c.stream);
+    if (e != cudaSuccess) return c.cuda_fail(e, "batch");
+    c.collect_kernel_stats();
+    c.arena.rewind(base);
+    for (uint32_t v : used) remap[v] = UINT32_MAX;
+    q0 = q;
+  }
+  return ENT_OK;
+}
+
 unsigned Ctx::persistent_grid(uint32_t n_work, const void* kern, int threads, size_t smem) {
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem) !=
@@ -831,21 +944,25 @@ unsigned Ctx::persistent_grid(uint32_t n_work, const void* kern, int threads, si
   return (unsigned)g;
 }
 
+// Adds the kernel times of the runs since the last collection (one engine
+// run, or one per batch of a job split into several) to the call's stats.
 void Ctx::collect_kernel_stats() {
   float ms = 0.f;
-  if (cudaEventElapsedTime(&ms, ev_k0, ev_k1) == cudaSuccess) stats.pair_kernel_ms = ms;
+  if (ran_k && cudaEventElapsedTime(&ms, ev_k0, ev_k1) == cudaSuccess) stats.pair_kernel_ms += ms;
+  ran_k = false;
   if (ran_m) {
-    if (cudaEventElapsedTime(&ms, ev_m[0][0], ev_m[0][1]) == cudaSuccess) stats.moment_edge_ms = ms;
+    if (cudaEventElapsedTime(&ms, ev_m[0][0], ev_m[0][1]) == cudaSuccess)
+      stats.moment_edge_ms += ms;
     if (cudaEventElapsedTime(&ms, ev_m[1][0], ev_m[1][1]) == cudaSuccess)
-      stats.moment_target_ms = ms;
+      stats.moment_target_ms += ms;
     ran_m = false;
   }
   for (int d = 0; d < 3; ++d) {
     if (ran_d[d] && cudaEventElapsedTime(&ms, ev_d[d][0], ev_d[d][1]) == cudaSuccess)
-      stats.pair_kernel_ms_by_dim[d] = ms;
+      stats.pair_kernel_ms_by_dim[d] += ms;
     ran_d[d] = false;
     if (pending_pairs) {
-      stats.candidate_pairs_by_dim[d] = h_nsrc_d[d];
+      stats.candidate_pairs_by_dim[d] += h_nsrc_d[d];
       stats.candidate_pairs += h_nsrc_d[d];
     }
   }
@@ -894,6 +1011,10 @@ int ent_create(ent_ctx** out, int device) {
     return ENT_ERR_CUDA;
   }
   if (const char* g = std::getenv("ENT_NO_GRAPHS")) c->use_graphs = (g[0] == '0');
+  if (const char* m = std::getenv("ENT_MAX_BATCH_INSTANCES")) {
+    const long v = std::strtol(m, nullptr, 10);
+    if (v >= 1 && v <= 65535) c->max_batch_instances = (uint32_t)v;
+  }
   if (init_log_table(&c->d_logtab) != cudaSuccess) {
     cudaGetLastError();
     ent_destroy(reinterpret_cast<ent_ctx*>(c));

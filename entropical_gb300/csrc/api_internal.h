@@ -22,11 +22,20 @@ struct Arena {
   std::vector<Block> blocks;
   size_t used_in_last = 0;
   size_t total_used = 0;
+  size_t peak = 0;  // largest total_used since the last reset
   void* alloc(size_t bytes);
   void reset();
-  void coalesce();  // one block of the current use's size (contents discarded)
+  void coalesce();  // one block of this call's peak use (contents discarded)
   void release();
-  size_t spare() const;  // bytes left in the blocks already held
+  size_t spare() const;  // bytes the next allocations get without cudaMalloc
+  // Rewinding to a mark gives back what was allocated after it; blocks added
+  // since are freed but the last, which is kept empty. Only while nothing
+  // in flight uses that memory (the stream idle).
+  struct Mark {
+    size_t n_blocks, used_in_last, total_used;
+  };
+  Mark mark() const { return {blocks.size(), used_in_last, total_used}; }
+  void rewind(const Mark& m);
 };
 
 struct Ctx {
@@ -43,6 +52,7 @@ struct Ctx {
   // strip moments: edge (symmetric) kernel and target kernel
   cudaEvent_t ev_m[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
   bool ran_m = false;
+  bool ran_k = false;  // ev_k0 / ev_k1 bracket this call's pair kernels
   uint64_t h_nsrc_d[3] = {0, 0, 0};
   Arena arena;
   std::string last_error;
@@ -71,6 +81,9 @@ struct Ctx {
   bool moment_auto = true;
   uint32_t moment_cells = 3;  // strips per bandwidth of PAIR_MOMENT (2..12)
   bool use_graphs = true;       // capture the batch kernel sequence in a CUDA graph
+  // Instances of one engine run (at most 65535); an estimator job with more,
+  // or more than the device's free memory holds, runs as several batches.
+  uint32_t max_batch_instances = 65535;
   // The batch's executable graph, kept across calls: a later batch is
   // captured again and, when its kernel sequence has the same shape, the
   // executable is updated in place (cudaGraphExecUpdate: new pointers, sizes
@@ -155,8 +168,21 @@ struct Engine {
   uint32_t group_base[4] = {0, 0, 0, 0};
   uint32_t group_slots[4] = {0, 0, 0, 0};
   int run(Ctx& c, const std::vector<ViewSpec>& views,
-          std::vector<InstSpec>& insts, uint32_t mode, EngineOut* out);
+          const std::vector<InstSpec>& insts, uint32_t mode, EngineOut* out);
 };
+
+// Runs `insts` as one engine batch when the job fits one (at most
+// c.max_batch_instances instances and 65535 views, its estimated workspace
+// within the device's free memory), else as consecutive batches of as many
+// instances as fit, each with the views it uses. After each run,
+// done(first, count, out) gets the run's instances [first, first + count)
+// and its EngineOut (slot_order indexes the run's instances). Between runs
+// of a split job the stream is synchronised and the run's workspace given
+// back; the single run returns with its work in flight, as Engine::run does.
+typedef int (*BatchDone)(void* arg, size_t first, size_t count, const EngineOut& out);
+int run_engine_batches(Ctx& c, const std::vector<ViewSpec>& views,
+                       const std::vector<InstSpec>& insts, uint32_t mode, BatchDone done,
+                       void* arg);
 
 int validate_selection(Ctx& c, size_t n_rows, size_t n_cols,
                        const uint32_t* i_cols, const float* h,

@@ -1,6 +1,7 @@
 // Batched estimators: all-pairs mutual information and uneven entropy
 // batches, each run as ONE engine batch, i.e. one persistent pair-kernel
-// launch per dimension over every (instance, tile) work item.
+// launch per dimension over every (instance, tile) work item (a job larger
+// than one batch holds runs as several).
 //
 // Replaces the per-call loops of the reference estimators: Mi::main
 // (mi.cpp:37-59) computes 1-D marginals inside its pair loop (M^2 1-D
@@ -23,35 +24,42 @@ using namespace ent;
 
 namespace {
 
-// Runs the engine in log-sum (or support-count) mode and returns, per
-// instance, -mean(log p) (or the in-support pair count).
-int run_entropies(Ctx& c, const std::vector<ViewSpec>& views,
-                  std::vector<InstSpec>& insts, bool counts,
-                  std::vector<double>* H) {
-  Engine eng;
-  EngineOut eo;
-  const uint32_t mode = counts ? (DM_COUNT | DM_SUMV) : DM_LOGSUM;
-  if (counts)
-    for (auto& s : insts) s.norm = 1.0;
-  int s = eng.run(c, views, insts, mode, &eo);
-  if (s) return s;
-  std::vector<double> ls(insts.size());
-  cudaError_t e = cudaMemcpyAsync(ls.data(), eo.d_logsum_sorted,
-                                  sizeof(double) * insts.size(),
+struct EntropyRun {
+  Ctx* c;
+  const std::vector<InstSpec>* insts;
+  bool counts;
+  std::vector<double>* H;
+};
+
+// The log-sums (or counts) of one engine run, by instance.
+int entropy_run_done(void* arg, size_t first, size_t count, const EngineOut& eo) {
+  EntropyRun& r = *static_cast<EntropyRun*>(arg);
+  Ctx& c = *r.c;
+  std::vector<double> ls(count);
+  cudaError_t e = cudaMemcpyAsync(ls.data(), eo.d_logsum_sorted, sizeof(double) * count,
                                   cudaMemcpyDeviceToHost, c.stream);
   if (e != cudaSuccess) return c.cuda_fail(e, "read log-sums");
   e = cudaStreamSynchronize(c.stream);
   if (e != cudaSuccess) return c.cuda_fail(e, "batch");
-  H->assign(insts.size(), 0.0);
-  for (size_t r = 0; r < insts.size(); ++r) {
-    const uint32_t i = eo.slot_order[r];
-    if (counts) {
-      (*H)[i] = ls[r];
-    } else {
-      (*H)[i] = -ls[r] / (double)insts[i].n;
-    }
+  for (size_t k = 0; k < count; ++k) {
+    const size_t i = first + eo.slot_order[k];
+    (*r.H)[i] = r.counts ? ls[k] : -ls[k] / (double)(*r.insts)[i].n;
   }
   return ENT_OK;
+}
+
+// Runs the engine in log-sum (or support-count) mode and returns, per
+// instance, -mean(log p) (or the in-support pair count); as one batch, or as
+// several for a job larger than one batch holds.
+int run_entropies(Ctx& c, const std::vector<ViewSpec>& views,
+                  std::vector<InstSpec>& insts, bool counts,
+                  std::vector<double>* H) {
+  const uint32_t mode = counts ? (DM_COUNT | DM_SUMV) : DM_LOGSUM;
+  if (counts)
+    for (auto& s : insts) s.norm = 1.0;
+  H->assign(insts.size(), 0.0);
+  EntropyRun r{&c, &insts, counts, H};
+  return run_engine_batches(c, views, insts, mode, entropy_run_done, &r);
 }
 
 // The densities of an all-pairs MI in batch order: the n_cols 1-D

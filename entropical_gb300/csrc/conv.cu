@@ -579,6 +579,7 @@ int hestimate_engine(Ctx& c, const float* raw, const std::vector<uint64_t>& raw_
     c.stats.kernel_launches += 3 * max_levels;
   }
   cudaEventRecord(c.ev_k1, s);
+  c.ran_k = true;
 
   std::vector<HestState> hs(nc);
   e = cudaMemcpyAsync(hs.data(), dst, sizeof(HestState) * nc, cudaMemcpyDeviceToHost, s);

@@ -1,4 +1,5 @@
-// The reference's estimator formulas on the device, each as ONE batch.
+// The reference's estimator formulas on the device, each as ONE batch (as
+// several for a job larger than one batch holds).
 //
 // The reference's estimator mains loop over columns / pairs, call
 // combined_densities() once per density (each a separate device allocation,
@@ -193,8 +194,7 @@ struct Batch {
     dens = static_cast<double*>(c.arena.alloc(sizeof(double) * std::max<size_t>(total, 1)));
     if (!dens) return c.fail(ENT_ERR_CUDA, "out of device memory");
     for (size_t i = 0; i < insts.size(); ++i) insts[i].out = dens + out_off[i];
-    Engine eng;
-    return eng.run(c, vt.views, insts, DM_WRITE_F64, nullptr);
+    return run_engine_batches(c, vt.views, insts, DM_WRITE_F64, nullptr, nullptr);
   }
 };
 
@@ -451,7 +451,6 @@ int ent_dens_all(ent_ctx* ctx, const float* coords, size_t n_rows, size_t n_cols
   if ((size_t)mx >= n_rows) return c.fail(ENT_ERR_ARG, "lag >= n_rows");
   const size_t M = n_cols;
   size_t n_inst = dims == 1 ? M : (dims == 2 ? M * (M - 1) / 2 : M * (M - 1) * (M - 2) / 6);
-  if (n_inst > 65535) return c.fail(ENT_ERR_TOO_LARGE, "more than 65535 densities");
   const size_t n_sel = n_rows - mx;
   if (n_inst_out) *n_inst_out = n_inst;
   if (n_sel_out) *n_sel_out = n_sel;
@@ -485,11 +484,15 @@ int ent_dens_all(ent_ctx* ctx, const float* coords, size_t n_rows, size_t n_cols
   for (size_t i = 0; i < n_inst; ++i) all[i] = (uint32_t)i;
   double* d_sums = nullptr;
   if ((s = instance_sums(B, all, &d_sums))) return s;
-  dim3 grid((unsigned)std::min<size_t>((n_sel + 255) / 256, 64), (unsigned)n_inst);
-  k_divide_rows<<<grid, 256, 0, c.stream>>>(B.dens, (uint32_t)n_sel, d_sums);
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = cudaSuccess;
+  for (size_t r0 = 0; r0 < n_inst && e == cudaSuccess; r0 += 65535) {  // grid y: 65535 rows
+    const size_t nr = std::min<size_t>(65535, n_inst - r0);
+    dim3 grid((unsigned)std::min<size_t>((n_sel + 255) / 256, 64), (unsigned)nr);
+    k_divide_rows<<<grid, 256, 0, c.stream>>>(B.dens + r0 * n_sel, (uint32_t)n_sel, d_sums + r0);
+    e = cudaGetLastError();
+    c.stats.kernel_launches += 1;
+  }
   if (e != cudaSuccess) return c.cuda_fail(e, "normalise");
-  c.stats.kernel_launches += 1;
   e = cudaMemcpyAsync(out, B.dens, sizeof(double) * n_inst * n_sel,
                       (flags & ENT_BATCH_DEVICE_OUTPUT) ? cudaMemcpyDeviceToDevice
                                                         : cudaMemcpyDeviceToHost,

@@ -185,6 +185,15 @@ int ent_support_counts(ent_ctx* ctx, const float* coords, size_t n_rows,
 
 /* ------------------------------------------------------------ batches */
 
+/*
+ * A batched job runs as one batch (one persistent pair-kernel launch per
+ * dimension over all its densities) when it fits one: at most 65535
+ * densities and its workspace within the device's free memory. A larger job
+ * runs as consecutive batches of as many densities as fit, with the same
+ * results. ENT_MAX_BATCH_INSTANCES (1..65535) in the environment when a
+ * context is created lowers the densities per batch of that context.
+ */
+
 /* flags for the batched entry points */
 #define ENT_BATCH_SUPPORT_COUNTS 2u /* return in-support pair counts instead
                                        of entropies (pair-rate reporting) */
@@ -395,8 +404,8 @@ int ent_reference_estimator(ent_ctx* ctx, const float* coords, size_t n_rows,
  * (dims = 2) or triple (dims = 3, the "dens -D 3" mode) in the reference's
  * order (i < j < k), each over lags taus[0..dims) (NULL: none; ignored for
  * dims = 1). out: *n_inst rows of *n_sel = n_rows - max(taus) values, host
- * memory, or device memory with ENT_BATCH_DEVICE_OUTPUT. At most 65535
- * densities per call.
+ * memory, or device memory with ENT_BATCH_DEVICE_OUTPUT. Every density of
+ * the call is held in device memory (*n_inst x *n_sel doubles).
  */
 int ent_dens_all(ent_ctx* ctx, const float* coords, size_t n_rows, size_t n_cols,
                  const float* h, uint32_t dims, const uint32_t* taus,
