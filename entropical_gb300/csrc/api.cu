@@ -850,10 +850,9 @@ size_t inst_bytes(const InstSpec& s) {
   return (size_t)s.n * kBatchBytesPerPoint[std::min(s.d, 3u)] + kBatchBytesPerInstance;
 }
 
-// What an engine run may take: the device's free memory and the workspace
-// already held, less an eighth (at least 2 GB) for the allocator's rounding,
-// graphs and other work on the device.
-size_t batch_budget(Ctx& c) {
+}  // namespace
+
+size_t device_budget(Ctx& c) {
   size_t free_b = 0, total_b = 0;
   if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
     cudaGetLastError();
@@ -864,8 +863,6 @@ size_t batch_budget(Ctx& c) {
   return avail > reserve ? avail - reserve : avail / 2;
 }
 
-}  // namespace
-
 int run_engine_batches(Ctx& c, const std::vector<ViewSpec>& views,
                        const std::vector<InstSpec>& insts, uint32_t mode, BatchDone done,
                        void* arg) {
@@ -875,7 +872,7 @@ int run_engine_batches(Ctx& c, const std::vector<ViewSpec>& views,
   for (const auto& v : views) est += (size_t)v.n * kBatchBytesPerViewPoint;
   const bool one_run = insts.size() <= c.max_batch_instances && views.size() <= kBatchMaxViews;
   size_t budget = SIZE_MAX;
-  if (!one_run || est > c.arena.spare()) budget = batch_budget(c);
+  if (!one_run || est > c.arena.spare()) budget = device_budget(c);
   if (one_run && est <= budget) {
     Engine eng;
     EngineOut eo;

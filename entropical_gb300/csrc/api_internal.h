@@ -180,6 +180,11 @@ struct Engine {
 // of a split job the stream is synchronised and the run's workspace given
 // back; the single run returns with its work in flight, as Engine::run does.
 typedef int (*BatchDone)(void* arg, size_t first, size_t count, const EngineOut& out);
+
+// Device memory one batch or pass may take: the device's free memory and the
+// workspace already held, less an eighth (at least 2 GB) for the allocator's
+// rounding, graphs and other work on the device.
+size_t device_budget(Ctx& c);
 int run_engine_batches(Ctx& c, const std::vector<ViewSpec>& views,
                        const std::vector<InstSpec>& insts, uint32_t mode, BatchDone done,
                        void* arg);

@@ -20,6 +20,8 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <cstddef>
+#include <cstdint>
 #include <vector>
 
 #include "../../include/entropical_gb300.h"
@@ -476,10 +478,13 @@ T* upload(Ctx& c, const std::vector<T>& v, cudaError_t* e) {
 // Shared implementation of ent_epa_convolution / ent_hestimate. `raw` holds
 // n_cols device columns back to back (raw_off offsets). mode: 0 = fixed
 // bandwidths h_fixed (convolution only), 1 = full search, 2 = warm search.
-int hestimate_engine(Ctx& c, const float* raw, const std::vector<uint64_t>& raw_off,
-                     const std::vector<uint32_t>& lens, int mode, const float* h_fixed_or_init,
-                     int skip, float* h_out, float* conv_out, ent_hest_stats* stats,
-                     const float* d_log_ratio) {
+namespace {
+
+// One pass of the search over at most kHestMaxCols columns, all held at once.
+int hestimate_pass(Ctx& c, const float* raw, const std::vector<uint64_t>& raw_off,
+                   const std::vector<uint32_t>& lens, int mode, const float* h_fixed_or_init,
+                   int skip, float* h_out, float* conv_out, ent_hest_stats* stats,
+                   const float* d_log_ratio) {
   cudaError_t e;
   const cudaStream_t s = c.stream;
   const uint32_t nc = (uint32_t)lens.size();
@@ -490,7 +495,6 @@ int hestimate_engine(Ctx& c, const float* raw, const std::vector<uint64_t>& raw_
   SortedViews sv;
   int rs = sort_views(c, views, &sv);
   if (rs) return rs;
-  if (nc > 65535u) return c.fail(ENT_ERR_TOO_LARGE, "too many columns in one search");
   std::vector<ConvCol> hc(nc);
   uint32_t slots = 0, chunks = 0;
   std::vector<uint32_t> base(nc);
@@ -613,14 +617,64 @@ int hestimate_engine(Ctx& c, const float* raw, const std::vector<uint64_t>& raw_
       }
       std::vector<float> h2(redo.size());
       std::vector<ent_hest_stats> st2(redo.size());
-      int r2 = hestimate_engine(c, raw, off2, len2, 1, nullptr, 0, h2.data(), nullptr,
-                                st2.data(), nullptr);
+      int r2 = hestimate_pass(c, raw, off2, len2, 1, nullptr, 0, h2.data(), nullptr,
+                              st2.data(), nullptr);
       if (r2) return r2;
       for (size_t q = 0; q < redo.size(); ++q) {
         h_out[redo[q]] = h2[q];
         if (stats) stats[redo[q]].conv_evals += st2[q].conv_evals;
       }
     }
+  }
+  return ENT_OK;
+}
+
+// Columns of one pass: the per-column kernels index columns by the grid's y
+// dimension. Device bytes per point of a column in a pass (its sort keys and
+// order with their ping-pong buffers, the sorted copy, the FP64 prefix sums)
+// and per column (search state, tile sums, convolution values).
+constexpr uint32_t kHestMaxCols = 65535;
+constexpr size_t kHestBytesPerPoint = 28;
+constexpr size_t kHestBytesPerCol = 1024;
+
+}  // namespace
+
+// A search over more columns than one pass takes, or than the device's free
+// memory holds at once, runs as consecutive passes over groups of columns,
+// the workspace rewound after each (every pass ends synchronised).
+int hestimate_engine(Ctx& c, const float* raw, const std::vector<uint64_t>& raw_off,
+                     const std::vector<uint32_t>& lens, int mode, const float* h_fixed_or_init,
+                     int skip, float* h_out, float* conv_out, ent_hest_stats* stats,
+                     const float* d_log_ratio) {
+  const size_t nc = lens.size();
+  size_t est = 0;
+  for (uint32_t n : lens) est += kHestBytesPerPoint * n + kHestBytesPerCol;
+  size_t budget = SIZE_MAX;
+  if (nc > kHestMaxCols || est > c.arena.spare()) budget = device_budget(c);
+  if (nc <= kHestMaxCols && est <= budget)
+    return hestimate_pass(c, raw, raw_off, lens, mode, h_fixed_or_init, skip, h_out, conv_out,
+                          stats, d_log_ratio);
+  const Arena::Mark base = c.arena.mark();
+  for (size_t q0 = 0; q0 < nc;) {
+    size_t q = q0, bytes = 0;
+    for (; q < nc; ++q) {
+      const size_t add = kHestBytesPerPoint * lens[q] + kHestBytesPerCol;
+      if (q > q0 && (bytes + add > budget || q - q0 >= kHestMaxCols)) break;
+      bytes += add;
+    }
+    const std::vector<uint64_t> off(raw_off.begin() + (std::ptrdiff_t)q0,
+                                    raw_off.begin() + (std::ptrdiff_t)q);
+    const std::vector<uint32_t> len(lens.begin() + (std::ptrdiff_t)q0,
+                                    lens.begin() + (std::ptrdiff_t)q);
+    int s = hestimate_pass(c, raw, off, len, mode, h_fixed_or_init ? h_fixed_or_init + q0 : nullptr,
+                           skip, h_out + q0, conv_out ? conv_out + q0 : nullptr,
+                           stats ? stats + q0 : nullptr, d_log_ratio ? d_log_ratio + q0 : nullptr);
+    if (s) return s;
+    const cudaError_t e = cudaStreamSynchronize(c.stream);
+    if (e != cudaSuccess) return c.cuda_fail(e, "hestimate");
+    c.collect_kernel_stats();
+    c.arena.rewind(base);
+    q0 = q;
   }
   return ENT_OK;
 }

@@ -98,3 +98,17 @@ def test_hestimate_instance_batch(ctx):
         ref, _ = ctx.hestimate(x, HEST_AMISE)
         assert np.array_equal(h[q, :x.shape[0]], ref)
         assert np.all(h[q, x.shape[0]:] == 0)
+
+
+def test_hestimate_over_more_than_65535_columns(ctx):
+    """70,000 columns run as two passes (the per-column kernels index columns
+    by the grid's y dimension). Each column's search depends on that column
+    alone, so the bandwidths equal a search over a few of them, bit for bit."""
+    rng = np.random.default_rng(12)
+    x = (rng.standard_normal((70_000, 200)) * rng.uniform(0.5, 2.0, (70_000, 1))).astype(np.float32)
+    h, st = ctx.hestimate(x, HEST_AMISE)
+    assert h.shape == (70_000,) and np.all(h > 0) and np.all(np.isfinite(h))
+    assert all(s["conv_evals"] > 0 for s in st[::997])
+    pick = [0, 1, 65_534, 65_535, 69_999]
+    h5, _ = ctx.hestimate(x, HEST_AMISE, cols=pick)
+    assert np.array_equal(h[pick], h5)
