@@ -464,8 +464,8 @@ typedef struct {
  * Per-column bandwidths of the selected columns cols[0..n_sel) (all columns
  * if cols is NULL), every column searched at once on the device (in passes
  * of at most 65535 columns, and of what the device's free memory holds,
- * when there are more; each column's result is independent of the others'). Replaces
- * Hestimate::main<KRNL> (hestimate.hxx:6-26) with Thumb::Kernel or
+ * when there are more; each column's result is independent of the others').
+ * Replaces Hestimate::main<KRNL> (hestimate.hxx:6-26) with Thumb::Kernel or
  * AmiseMin::Kernel. h_init (warm mode): one start value per selected column.
  * stats (nullable): one entry per selected column. Host memory.
  */
