@@ -112,8 +112,6 @@ __global__ void k_gather_sorted(const ConvCol* __restrict__ cols,
     xs[k] = k < C.n ? x[p[k]] : 0.f;
 }
 
-__device__ __forceinline__ float piv_of(double a, double b) { return (float)(a + b); }
-
 // Start a full search (hestimate.cpp:101-103) or a warm one: descend
 // `skip` levels of the same dyadic bracket tree towards h_init without
 // evaluating anything, then search from there.

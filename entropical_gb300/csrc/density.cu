@@ -814,7 +814,7 @@ int density_r_supported(int d, int r) {
   return 0;
 }
 
-int density_tile_targets(int d, int r) { return 4 * r; }
+int density_tile_targets(int /*d*/, int r) { return 4 * r; }
 
 cudaError_t launch_colstats(cudaStream_t st, const ViewDev* views,
                             uint32_t n_views, ViewStats* stats) {

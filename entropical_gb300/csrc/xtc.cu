@@ -999,7 +999,8 @@ int ent_read_xtc(ent_ctx* ctx, const char* path, const size_t* usecols, size_t n
 int ent_write_xtc(const char* path, const float* coords, size_t n_rows, size_t n_cols,
                   char primary_index, float precision) {
   g_xtc_error.clear();
-  if (!path || (!coords && n_rows * n_cols) || (primary_index != 'C' && primary_index != 'R'))
+  if (!path || (!coords && n_rows != 0 && n_cols != 0) ||
+      (primary_index != 'C' && primary_index != 'R'))
     return ENT_ERR_ARG;
   if (n_cols == 0 || n_cols % 3 != 0 || n_cols / 3 > (size_t)INT_MAX || n_rows > (size_t)INT_MAX) {
     g_xtc_error = "columns must be a positive multiple of 3 (x, y, z per atom)";
