@@ -1,4 +1,5 @@
-"""The FP64 MLP oracle itself: analytic gradients against finite differences."""
+"""The FP64 MLP oracle itself: analytic gradients against finite differences;
+and the committed network weights run through it on the CPU."""
 import numpy as np
 
 from oracle import mlp_ref as R
@@ -23,3 +24,23 @@ def test_oracle_gradient_finite_differences():
         lp, _ = R.loss_and_grad(p.astype(np.float64) + e, mu, sd, X, T, M)
         lm, _ = R.loss_and_grad(p.astype(np.float64) - e, mu, sd, X, T, M)
         assert abs((lp - lm) / 2e-3 - g[i]) < 1e-6 * max(1, abs(g[i])) + 1e-7
+
+
+def test_shipped_network_predicts_the_searchs_constant_ratio():
+    """The committed weights (entropical_gb300/data/bandwidth_mlp.npz) have the
+    library's layout, and the FP64 oracle forward pass on oracle features of
+    fresh mixtures predicts log(h / h0) = log(2 - 1.9/512) for every used
+    dimension: the reference's AMISE search always returns that ratio, since
+    its objective falls monotonically in h, so that is what the network learned."""
+    from entropical_gb300 import _native, learned, workloads
+    z = np.load(learned.DEFAULT_WEIGHTS)
+    assert z["params"].shape == (int(_native.load().ent_mlp_param_count()),) == (21123,)
+    assert z["mu"].shape == z["sd"].shape == (32,)
+    assert np.all(np.isfinite(z["params"])) and np.all(z["sd"] > 0)
+    rng = np.random.default_rng(3)
+    target = np.log(learned.CONSTANT_RATIO)
+    for q in range(9):
+        d = 1 + q % 3
+        x = workloads.mixture_instance(rng, d, 3000)
+        y = R.forward(z["params"], z["mu"], z["sd"], R.features(x)[None].astype(np.float32))[3][0]
+        assert np.all(np.abs(y[:d] - target) < 1e-4), (d, y)
